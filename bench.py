@@ -1,0 +1,384 @@
+#!/usr/bin/env python
+"""TOF list-mode OSEM throughput on the clinical-size workload.
+
+Workload (one "step" = one full OSEM iteration = 10 subsets over all events):
+  scanner  424/444 mm radii, 48 blocks/ring of 13 x 13 crystals (4 mm), 4 block rings
+           (32,448 crystals); TOF 530 ps FWHM (sigma 33.7 mm along the LOR), Gaussian truncated at
+           3 sigma; LORs float32 (N, 7), TOF column in mm
+  events   2e7, seeded synthetic: water-ellipsoid body (30 x 20 x 100 cm axes) with 0..40 random
+           hot/cold ellipsoids (contrast 0.2..8), isotropic emission, hits snapped to crystals
+  image    200 x 200 x 109 float32 at 2.04 x 2.04 x 2.03 mm; sensitivity image precomputed on the
+           GPU from all 1.05e9 ordered crystal pairs (timed separately, reported as emap_s)
+  update   MlemFullTof's rule per subset (div_no_nan(y, p + 1e-5), x * bp / emap) with the
+           sensitivity scaled by 1/n_subsets
+Metric: LOR-voxel updates/s = (projector + backprojector (LOR, voxel) visits per iteration) /
+seconds per iteration; visits are counted exactly by srf_count_pairs.
+
+--impl reference runs the reference's CPU arithmetic (the oracle's restatement of
+srfnef's Siddon device functions, with all host threads) on a bounded sample of the same
+workload and reports the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TOF OSEM s/iter & LOR-voxel updates/s on 1 GB300 vs plain, rel L2 err ≤1e-5"
+UNIT = "LOR-voxel updates/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--events", type=float, default=2e7)
+    ap.add_argument("--subsets", type=int, default=10)
+    ap.add_argument("--nsigma", type=float, default=3.0)
+    ap.add_argument("--lanes", type=int, default=32)
+    ap.add_argument("--cpu-sample", type=int, default=400000)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--seed", type=int, default=20250101)
+    return ap.parse_args()
+
+
+def workload_config(a):
+    return {
+        "workload": "tof_listmode_osem_clinical",
+        "events": int(a.events), "image": [200, 200, 109], "voxel_mm": [2.04, 2.04, 2.03],
+        "crystals": 32448, "subsets": a.subsets, "tof_fwhm_ps": 530.0, "tof_nsigma": a.nsigma,
+        "step": "one full OSEM iteration (all subsets)",
+        "l2": "inputs larger than L2 (LOR stream 560 MB per iteration)",
+        "lanes_per_lor": a.lanes,
+    }
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.path = None
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(gpu_index)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(a):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if a.impl == "gb300" else "gloo"
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, ws, device=None):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(v, ws, device=None):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU (oracle) timing
+
+def cpu_sample_rate(lors_np, x_np, ic, tof, nsigma, threads):
+    """(pairs per second, pairs, seconds) of one fused subset pass (projection, ratio,
+    backprojection) of the oracle over lors_np."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle as O
+    O.build()
+    kw = dict(tof=True, tof_bin=tof[0], tof_sigma2=tof[1], tof_nsigma=nsigma, threads=threads)
+    t0 = time.perf_counter()
+    p, n1 = O.trace(lors_np, ic.shape, ic.center, ic.size, O.RULES_PROJ, O.GATHER, image=x_np, **kw)
+    r = O.ratio(np.ones(len(p), np.float32), p, "full_tof")
+    _, n2 = O.trace(lors_np, ic.shape, ic.center, ic.size, O.RULES_BACK, O.SCATTER, values=r, **kw)
+    dt = time.perf_counter() - t0
+    return (n1 + n2) / dt, n1 + n2, dt
+
+
+def make_workload(a, device, rank):
+    import torch
+    from srf_gb300 import synth
+    sc, ic = synth.scanner_clinical(), synth.image_clinical()
+    act = synth.phantom_body(ic, seed=a.seed + 7, device=device)
+    lors = synth.sample_events(sc, ic, act, int(a.events), seed=a.seed + rank, tof_fwhm_ps=530.0,
+                               device=device)
+    return sc, ic, act, lors
+
+
+def run_reference(a, ws, rank):
+    """Reference arm: the reference's Siddon arithmetic on the host cores (oracle port)."""
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+    from srf_gb300 import synth
+    sc, ic = synth.scanner_clinical(), synth.image_clinical()
+    n = int(a.cpu_sample)
+    act = synth.phantom_body(ic, seed=a.seed + 7)
+    lors = synth.sample_events(sc, ic, act, n, seed=a.seed, tof_fwhm_ps=530.0).numpy()
+    x = np.ones(ic.shape, dtype=np.float32)
+    tof = (sc.tof.tof_bin, sc.tof.tof_sigma2)
+    threads = os.cpu_count() or 1
+    for _ in range(a.warmup):
+        cpu_sample_rate(lors[: max(1000, n // 20)], x, ic, tof, a.nsigma, threads)
+    rates, secs = [], []
+    for _ in range(a.steps):
+        r, pairs, dt = cpu_sample_rate(lors, x, ic, tof, a.nsigma, threads)
+        rates.append(r)
+        secs.append(dt)
+    val = statistics.median(rates)
+    sample = (f"{n} of {int(a.events)} events per step: one TOF subset pass (projection, ratio, "
+              f"backprojection) of the oracle restatement of srfnef's Siddon device functions")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * statistics.median(secs),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": workload_config(a),
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    ws, rank, local = dist_setup(a)
+    if a.impl == "reference":
+        run_reference(a, ws, rank)
+        return
+    import numpy as np
+    import torch
+    from srf_gb300 import _lib, kernels, synth
+    from srf_gb300._lib import SRF_RATIO_DIV_NO_NAN
+    from srf_gb300.emap_generator import EmapGenerator
+    from srf_gb300.geometry import block_full_crystal_table
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.load()
+    _lib.set_group_lanes(a.lanes)
+
+    sc, ic, act, lors = make_workload(a, dev, rank)
+    tof = (sc.tof.tof_bin, sc.tof.tof_sigma2)
+    n = lors.shape[0]
+    n_sub = a.subsets
+    n_per = n // n_sub
+
+    # sensitivity image over all crystal pairs (timed separately)
+    table = torch.as_tensor(block_full_crystal_table(sc), device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    emap = kernels.emap_block_full(table, sc.nb_blocks_per_ring, ic.shape, ic.center, ic.size)
+    torch.cuda.synchronize()
+    emap_s = time.perf_counter() - t0
+    em = (emap * (1.0 / n_sub)).permute(2, 1, 0).contiguous().permute(2, 1, 0)
+
+    # subset order: a seeded permutation, each subset contiguous
+    perm = torch.as_tensor(np.random.default_rng(a.seed).permutation(n), device=dev)
+    lors = lors.index_select(0, perm).contiguous()
+    del perm
+
+    # exact LOR-voxel visits of one iteration
+    p_fwd = kernels.count_pairs(lors, ic.shape, ic.center, ic.size, rules=0, tof=tof, tof_nsigma=a.nsigma)
+    p_bwd = kernels.count_pairs(lors, ic.shape, ic.center, ic.size, rules=1, tof=tof, tof_nsigma=a.nsigma)
+    updates_per_iter = p_fwd + p_bwd
+
+    st = kernels.SubsetState(ic.shape, ic.center, ic.size, dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def iteration(lors_dev, ev=None):
+        for k in range(n_sub):
+            sl = lors_dev[k * n_per:(k + 1) * n_per]
+            if ev is not None:
+                ev[k][0].record(stream)
+            st.subset(sl, None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5, tof=tof, tof_nsigma=a.nsigma)
+            if ev is not None:
+                ev[k][1].record(stream)
+            st.update(em, guard_zero=True)
+
+    for _ in range(a.warmup):
+        iteration(lors)
+    torch.cuda.synchronize()
+
+    evs = [[[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
+            for _ in range(n_sub)] for _ in range(a.steps)]
+    clocks = Clocks(local)
+    barrier(ws)
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for s_ in range(a.steps):
+        iteration(lors, evs[s_])
+    stop.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop()
+    ms_total = start.elapsed_time(stop)
+    ms_total = max_over_ranks(ms_total, ws, dev)
+    ms_step = ms_total / a.steps
+    kern_ms = [evs[s_][k][0].elapsed_time(evs[s_][k][1]) for s_ in range(a.steps) for k in range(n_sub)]
+    kern_ms_avg = sum(kern_ms) / len(kern_ms)
+    total_updates = sum_over_ranks(float(updates_per_iter), ws, dev)
+    value = total_updates / (ms_step / 1000.0)
+
+    # roofline of the dominant kernel (fused subset step): algorithmic bytes per launch
+    # = LOR rows read + 4 B per projector visit (image read) + 8 B per backprojector visit (RMW)
+    stride_b = lors.stride(0) * 4
+    alg_bytes = (n_per * stride_b + 4.0 * p_fwd / n_sub + 8.0 * p_bwd / n_sub)
+    achieved = alg_bytes / (kern_ms_avg / 1000.0) / 1e9
+    peak, peak_kind = peaks()
+
+    # end to end through the public API: pinned host LORs -> device -> one iteration -> image back
+    e2e = None
+    if not a.no_e2e:
+        host = torch.empty(lors.shape, dtype=lors.dtype, pin_memory=True)
+        host.copy_(lors)
+        torch.cuda.synchronize()
+        dev_buf = torch.empty_like(lors)
+        out_host = torch.empty(ic.shape[::-1], dtype=torch.float32, pin_memory=True)
+        for _ in range(1):
+            dev_buf.copy_(host, non_blocking=True)
+            iteration(dev_buf)
+            out_host.copy_(st.x.permute(2, 1, 0), non_blocking=True)
+        torch.cuda.synchronize()
+        barrier(ws)
+        e_start, e_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e_start.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            dev_buf.copy_(host, non_blocking=True)
+            iteration(dev_buf)
+            out_host.copy_(st.x.permute(2, 1, 0), non_blocking=True)
+        e_stop.record(stream)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) / a.steps
+        e_ms = max(e_start.elapsed_time(e_stop) / a.steps, 1000 * wall)
+        e_ms = max_over_ranks(e_ms, ws, dev)
+        e2e = {"value": total_updates / (e_ms / 1000.0), "unit": UNIT,
+               "h2d_bytes_per_step": int(host.numel() * 4), "d2h_bytes_per_step": int(out_host.numel() * 4),
+               "ms_per_step": e_ms}
+        del host, dev_buf
+
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        samp = lors[: a.cpu_sample].cpu().numpy()
+        x_np = st.x.contiguous().cpu().numpy()
+        threads = 1
+        rate, pairs, dt = cpu_sample_rate(samp, x_np, ic, tof, a.nsigma, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{len(samp)} of {n} events: one TOF subset pass (projection, ratio, "
+                         f"backprojection) of the oracle, {pairs} visits in {dt:.2f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_step, "s_per_iter": ms_step / 1000.0,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded phantom, events snapped to crystals)",
+            "config": workload_config(a),
+            "updates_per_iter": updates_per_iter, "pairs_fwd": p_fwd, "pairs_bwd": p_bwd,
+            "emap_s": emap_s, "emap_lors": int(sc.nb_crystals) ** 2,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "k_osem_subset (fused projection+ratio+backprojection)",
+                         "launch_ms": kern_ms_avg, "alg_bytes_per_launch": alg_bytes,
+                         "peak_kind": peak_kind},
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": a.steps * n_sub * 2,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

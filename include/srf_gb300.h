@@ -1,0 +1,191 @@
+/* srf_gb300 -- C ABI of the GB300 (sm_103a) list-mode PET reconstruction hot path.
+ *
+ * Drop-in for the CUDA side of srfnef's Siddon TF ops and their callers. Every entry point takes
+ * plain device pointers, host-side sizes/parameters and a cudaStream_t (as void*, NULL = legacy
+ * default stream), launches asynchronously on that stream and returns an int status:
+ *   SRF_OK (0), or one of the SRF_E* codes below; srf_last_error() gives a message for the
+ *   calling thread. No entry point allocates device memory, copies parameters device->host or
+ *   synchronises, unless its comment says so.
+ *
+ * Conventions shared by the projector family:
+ *   lors        N LORs, row-major, `lor_stride` floats per LOR (>= 6): x1 y1 z1 x2 y2 z2 [...] in mm.
+ *   tof         TOF values in mm (d2 - d1), tof[i * tof_stride]; srfnef passes column 6 of its
+ *               (N, 7) Lors array (srfnef/data/lors.py:20-22), i.e. tof = lors + 6, stride 7.
+ *   grid        {nx, ny, nz}; center {cx, cy, cz} and size {sx, sy, sz} in mm (the image's
+ *               ``shape``, ``center`` and ``size``; srfnef passes them as three small tensors).
+ *   image       float32 voxels addressed ix*st[0] + iy*st[1] + iz*st[2] (element strides).
+ *               srfnef's ops take the x-fastest array st = {1, nx, nx*ny}.
+ *   image_t     optional second view of the same voxels used for y-dominant LORs; a y-fastest
+ *               copy (st = {ny, 1, nx*ny}) makes those LORs' memory accesses coalesced. NULL: the
+ *               first view serves all LORs. For backprojections image_t is a second accumulator
+ *               that receives the y-dominant LORs; the result is image + image_t (see
+ *               srf_fold_views), which the caller zeroes beforehand like image.
+ *   tof_nsigma  0 reproduces the reference's untruncated Gaussian; > 0 drops slabs whose TOF
+ *               argument exceeds tof_nsigma standard deviations (not in the reference).
+ */
+#ifndef SRF_GB300_H
+#define SRF_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SRF_OK 0
+#define SRF_EINVAL 1      /* null pointer, negative count, bad stride          */
+#define SRF_EGRID 2       /* non-positive or oversized grid, bad size/strides  */
+#define SRF_ENONFINITE 3  /* non-finite center/size/TOF parameter              */
+#define SRF_ECUDA 4       /* CUDA launch or runtime error                      */
+#define SRF_ERANGE 5      /* a size beyond a documented limit                  */
+
+/* Message for the last non-zero status returned on this thread ("" if none). */
+const char *srf_last_error(void);
+
+/* ABI version (major*100 + minor). */
+int srf_version(void);
+
+/* Lanes per LOR used by the traversal kernels (8, 16 or 32; default 32). Process-wide. */
+int srf_set_group_lanes(int lanes);
+
+/* ------------------------------------------------------------------ projector family */
+
+/* p[i] = sum_v A_iv image_v, non-TOF.
+ * Replaces the TF op "Projection" (srfnef/cc/siddon/siddon.cc:11-21, Compute :48-102) and its
+ * launcher projection() (srfnef/cc/siddon/siddon.cu.cc:706-728). out[N] is fully written (the
+ * op's memset is included). */
+int srf_projection(const float *lors, int64_t n, int32_t lor_stride,
+                   const float *image, const int64_t image_strides[3],
+                   const float *image_t, const int64_t image_t_strides[3],
+                   const int32_t grid[3], const float center[3], const float size[3],
+                   float *out, void *stream);
+
+/* image += A^T values, non-TOF (backprojector rules: no endpoint/steep skip, no 1/L^2).
+ * Replaces "Backprojection" (siddon.cc:23-35, Compute :104-161) and backprojection()
+ * (siddon.cu.cc:731-753). Accumulates; the op's memset is the caller's zero fill. */
+int srf_backprojection(const float *lors, int64_t n, int32_t lor_stride, const float *values,
+                       float *image, const int64_t image_strides[3],
+                       float *image_t, const int64_t image_t_strides[3],
+                       const int32_t grid[3], const float center[3], const float size[3],
+                       void *stream);
+
+/* TOF projection. Replaces "ProjectionTof" (srfnef/cc/siddon_tof/siddon_tof.cc:11-24,
+ * Compute :56-119) and projection() (srfnef/cc/siddon_tof/siddon_tof.cu.cc:761-785). */
+int srf_projection_tof(const float *lors, int64_t n, int32_t lor_stride,
+                       const float *tof, int32_t tof_stride,
+                       float tof_bin, float tof_sigma2, float tof_nsigma,
+                       const float *image, const int64_t image_strides[3],
+                       const float *image_t, const int64_t image_t_strides[3],
+                       const int32_t grid[3], const float center[3], const float size[3],
+                       float *out, void *stream);
+
+/* TOF backprojection. Replaces "BackprojectionTof" (siddon_tof.cc:26-41, Compute :121-188) and
+ * backprojection() (siddon_tof.cu.cc:787-812). Accumulates. */
+int srf_backprojection_tof(const float *lors, int64_t n, int32_t lor_stride,
+                           const float *tof, int32_t tof_stride,
+                           float tof_bin, float tof_sigma2, float tof_nsigma,
+                           const float *values,
+                           float *image, const int64_t image_strides[3],
+                           float *image_t, const int64_t image_t_strides[3],
+                           const int32_t grid[3], const float center[3], const float size[3],
+                           void *stream);
+
+/* image += P^T values for the projector P of srf_projection (tof == NULL) or
+ * srf_projection_tof: the exact adjoint (projector rules, 1/L^2 weights), used as the backward
+ * of the differentiable projector. The reference's backprojector is not this adjoint. */
+int srf_projection_adjoint(const float *lors, int64_t n, int32_t lor_stride,
+                           const float *tof, int32_t tof_stride,
+                           float tof_bin, float tof_sigma2, float tof_nsigma,
+                           const float *values,
+                           float *image, const int64_t image_strides[3],
+                           float *image_t, const int64_t image_t_strides[3],
+                           const int32_t grid[3], const float center[3], const float size[3],
+                           void *stream);
+
+/* *count += number of (LOR, voxel) weight visits the projector (rules 0) or backprojector
+ * (rules 1) rule set makes for these LORs (tof == NULL: non-TOF rules). `count` is a device
+ * unsigned 64-bit counter. These are the "LOR-voxel updates" of the throughput metric; the CPU
+ * oracle counts the same visits. No counterpart in the reference. */
+int srf_count_pairs(const float *lors, int64_t n, int32_t lor_stride,
+                    const float *tof, int32_t tof_stride,
+                    float tof_bin, float tof_sigma2, float tof_nsigma, int32_t rules,
+                    const int32_t grid[3], const float center[3], const float size[3],
+                    unsigned long long *count, void *stream);
+
+/* dst[v] += src_t[v] for two views of one grid (folds a y-fastest accumulator into dst). */
+int srf_fold_views(float *dst, const int64_t dst_strides[3], const float *src,
+                   const int64_t src_strides[3], const int32_t grid[3], void *stream);
+
+/* dst = src re-laid out (any strides to any strides), e.g. x-fastest -> y-fastest copy. */
+int srf_copy_view(float *dst, const int64_t dst_strides[3], const float *src,
+                  const int64_t src_strides[3], const int32_t grid[3], void *stream);
+
+/* ------------------------------------------------------------------ MLEM / OSEM */
+
+/* Ratio rules of the reference's update loops:
+ *  SRF_RATIO_DIV_NO_NAN : r = tf.div_no_nan(y, p + eps)  (MlemFull eps=0, mlem_full.py:68;
+ *                                                          MlemFullTof eps=1e-5, mlem_full_tof.py:64)
+ *  SRF_RATIO_PLAIN      : r = y / (p + eps)               (Mlem eps=mean(y)*1e-8, mlem.py:41-42;
+ *                                                          OsemFull eps=1e-8, osem_full.py:75-76) */
+#define SRF_RATIO_DIV_NO_NAN 0
+#define SRF_RATIO_PLAIN 1
+
+/* One fused subset step of list-mode MLEM/OSEM for the LORs given:
+ *   p_i = (A x)_i ; r_i = rule(y_i, p_i) ; bp += A_bp^T r
+ * in a single pass over the LORs (each LOR's projection, ratio and backprojection are computed
+ * back to back; p and r never reach memory). tof == NULL: non-TOF projector/backprojector pair of
+ * srf_projection/srf_backprojection; otherwise the TOF pair. y == NULL means y_i = 1 (list mode).
+ * x/x_t are read (x_t optional, y-fastest), bp/bp_t accumulate (bp_t optional, folded by
+ * srf_osem_update). loglik (optional, device double) += sum_i y_i * log(p_i + eps).
+ * Replaces the per-iteration bodies of mlem_full.py:66-70, mlem_full_tof.py:62-67,
+ * mlem.py:39-43 and osem_full.py:74-77 up to the image update. */
+int srf_osem_subset(const float *lors, int64_t n, int32_t lor_stride,
+                    const float *tof, int32_t tof_stride,
+                    float tof_bin, float tof_sigma2, float tof_nsigma,
+                    const float *y, int32_t ratio_rule, float eps,
+                    const float *x, const float *x_t, float *bp, float *bp_t,
+                    const int32_t grid[3], const float center[3], const float size[3],
+                    double *loglik, void *stream);
+
+/* Multiplicative update on x-fastest images (x_t/bp_t y-fastest, both optional):
+ *   x <- (x * (bp + bp_t)) / e,  e = emap (guard_zero: emap == 0 -> 1e8, mlem_full_tof.py:56-58)
+ * then x_t <- x (y-fastest copy) and bp, bp_t <- 0, ready for the next subset. */
+int srf_osem_update(float *x, float *x_t, float *bp, float *bp_t, const float *emap,
+                    int32_t guard_zero, const int32_t grid[3], void *stream);
+
+/* ------------------------------------------------------------------ sensitivity image */
+
+/* emap += sum over all ordered crystal pairs of the non-TOF backprojection of 1, generated on
+ * the device from a crystal table in srfnef's 'block-full' order (n_blocks * m rows, m crystals
+ * per block column; pairs (i*m+a, j*m+b) for all i, j, a, b, self pairs included), i.e.
+ * EcatEmapGenerator('block-full') (srfnef/functions/emap_generator.py:77-111) without the
+ * 2304 host-built LOR arrays. emap/emap_t as the backprojection views. */
+int srf_emap_block_full(const float *crystal_table, int32_t n_blocks, int32_t m,
+                        float *emap, const int64_t emap_strides[3],
+                        float *emap_t, const int64_t emap_t_strides[3],
+                        const int32_t grid[3], const float center[3], const float size[3],
+                        void *stream);
+
+/* ------------------------------------------------------------------ single-scatter simulation */
+
+/* Raw single-scatter sums for crystal pairs (loop_all_lors / loop_all_s / get_scale of
+ * srfnef/corrections/scattering/scatter_fraction/scatter_fraction.py:40-136 and fkn of
+ * kn_formula.py:6-20, including the reference's whole-degree angle quantisation and its use of
+ * the angle inside fkn):
+ *   pairs          int32 (a, b) crystal ids, n_pairs rows
+ *   crystal_pos    float32 (n_crystals, 3); scatter_pos float32 (n_scatter, 3)
+ *   sumup_emission, atten  float32 (n_crystals, n_scatter), crystal-major
+ *   umap           float32 (shape0, shape1, shape2) C order, umap_size mm
+ * Outputs scatter[k] and scale[k] before the host scaling of scatter_fraction.py:27-36. */
+int srf_sss(const int32_t *pairs, int64_t n_pairs, const float *crystal_pos, int32_t n_crystals,
+            const float *scatter_pos, int32_t n_scatter, const float *sumup_emission,
+            const float *atten, const float *umap, const int32_t umap_shape[3],
+            const float umap_size[3], int32_t nb_crystals_per_ring, int32_t nb_blocks_per_ring,
+            const int32_t grid_block[3], int32_t low_energy, int32_t high_energy,
+            float resolution, float *scatter, float *scale, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SRF_GB300_H */

@@ -1,0 +1,251 @@
+// Projector family: forward projection, backprojection, exact adjoint (non-TOF and TOF), and the
+// view fold/copy helpers. Kernels are grid-stride over LORs, G lanes per LOR (siddon.cuh).
+#include "common.cuh"
+
+namespace srf {
+
+enum Action : int { GATHER = 0, SCATTER = 1, COUNT = 2 };
+
+// Warp-uniform loop over LORs: each warp takes 32/G consecutive LORs per round, so the group
+// shuffles in group_sum always see all 32 lanes.
+template <int G, bool TOF, int RULES, int ACTION>
+__global__ void __launch_bounds__(kBlock)
+k_trace(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
+        int tof_stride, Grid g, TofParams tp, View v, View vt, const float *__restrict__ values,
+        float *__restrict__ out) {
+    constexpr int GPW = 32 / G;
+    const int lane = threadIdx.x & (G - 1);
+    const int gi = (threadIdx.x & 31) / G;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool have_t = vt.ptr != nullptr;
+    for (int64_t base = warp * GPW; base < n; base += nwarps * GPW) {
+        const int64_t i = base + gi;
+        const bool valid = i < n;
+        float acc = 0.0f;
+        if (valid) {
+            const float *l = lors + i * stride;
+            const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
+            LorSetup S;
+            if (setup_lor<TOF, RULES>(__ldg(l), __ldg(l + 1), __ldg(l + 2), __ldg(l + 3),
+                                      __ldg(l + 4), __ldg(l + 5), tv, g, tp, v.st, vt.st, have_t,
+                                      S)) {
+                float *im = (!S.xdom && have_t) ? vt.ptr : v.ptr;
+                if (ACTION == COUNT) {
+                    for (int ip = S.lo + lane; ip <= S.hi; ip += G)
+                        slab<TOF, RULES>(S, ip, [&](int32_t, float) { acc += 1.0f; });
+                } else if (ACTION == GATHER) {
+                    const float *imc = im;
+                    for (int ip = S.lo + lane; ip <= S.hi; ip += G)
+                        slab<TOF, RULES>(S, ip, [&](int32_t off, float w) { acc += __ldg(imc + off) * w; });
+                } else {
+                    const float val = __ldg(values + i);
+                    if (val != 0.0f)
+                        for (int ip = S.lo + lane; ip <= S.hi; ip += G)
+                            slab<TOF, RULES>(S, ip, [&](int32_t off, float w) { atomicAdd(im + off, val * w); });
+                }
+            }
+        }
+        if (ACTION == GATHER) {
+            acc = group_sum<G>(acc);
+            if (valid && lane == 0) out[i] = acc;
+        } else if (ACTION == COUNT) {
+            acc = group_sum<G>(acc);  // < 2^24 visits per LOR, exact in FP32
+            if (valid && lane == 0 && acc > 0.0f)
+                atomicAdd((unsigned long long *)out, (unsigned long long)acc);
+        }
+    }
+}
+
+template <int G, bool TOF, int RULES, int ACTION>
+static int launch_trace_g(const float *lors, int64_t n, int stride, const float *tof,
+                          int tof_stride, const Grid &g, const TofParams &tp, const View &v,
+                          const View &vt, const float *values, float *out, cudaStream_t s) {
+    auto kern = k_trace<G, TOF, RULES, ACTION>;
+    unsigned blocks = grid_for(kern, n, kBlock / G);
+    kern<<<blocks, kBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, v, vt, values, out);
+    return check_cuda("trace kernel launch");
+}
+
+template <bool TOF, int RULES, int ACTION>
+static int launch_trace(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                        const Grid &g, const TofParams &tp, const View &v, const View &vt,
+                        const float *values, float *out, cudaStream_t s) {
+    if (n == 0) return ok();
+    switch (group_lanes()) {
+    case 8: return launch_trace_g<8, TOF, RULES, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, values, out, s);
+    case 16: return launch_trace_g<16, TOF, RULES, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, values, out, s);
+    default: return launch_trace_g<32, TOF, RULES, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, values, out, s);
+    }
+}
+
+// Elementwise kernels over a grid with arbitrary views.
+__global__ void k_fold(float *dst, View d, const float *src, View sv, int nx, int ny, int nz) {
+    const int64_t total = (int64_t)nx * ny * nz;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t ix = k % nx, iy = (k / nx) % ny, iz = k / ((int64_t)nx * ny);
+        dst[ix * d.st[0] + iy * d.st[1] + iz * d.st[2]] += src[ix * sv.st[0] + iy * sv.st[1] + iz * sv.st[2]];
+    }
+}
+
+__global__ void k_copy(float *dst, View d, const float *src, View sv, int nx, int ny, int nz) {
+    const int64_t total = (int64_t)nx * ny * nz;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t ix = k % nx, iy = (k / nx) % ny, iz = k / ((int64_t)nx * ny);
+        dst[ix * d.st[0] + iy * d.st[1] + iz * d.st[2]] = src[ix * sv.st[0] + iy * sv.st[1] + iz * sv.st[2]];
+    }
+}
+
+}  // namespace srf
+
+using namespace srf;
+
+extern "C" {
+
+const char *srf_last_error(void) { return g_err; }
+
+int srf_version(void) { return 100; }
+
+int srf_set_group_lanes(int lanes) {
+    if (lanes != 8 && lanes != 16 && lanes != 32) return fail(SRF_EINVAL, "lanes must be 8, 16 or 32");
+    group_lanes() = lanes;
+    return ok();
+}
+
+static int common_args(const float *lors, int64_t n, int32_t lor_stride, const void *image,
+                       const int64_t *st, const void *image_t, const int64_t *st_t,
+                       const int32_t grid[3], const float center[3], const float size[3], Grid &g,
+                       View &v, View &vt) {
+    int rc;
+    if ((rc = check_lors(lors, n, lor_stride))) return rc;
+    if ((rc = check_geometry(grid, center, size, g))) return rc;
+    if ((rc = check_view(image, st, g, "image", v, true))) return rc;
+    if ((rc = check_view(image_t, st_t, g, "image_t", vt, false))) return rc;
+    return SRF_OK;
+}
+
+int srf_projection(const float *lors, int64_t n, int32_t lor_stride, const float *image,
+                   const int64_t image_strides[3], const float *image_t,
+                   const int64_t image_t_strides[3], const int32_t grid[3], const float center[3],
+                   const float size[3], float *out, void *stream) {
+    Grid g; View v, vt; int rc;
+    if ((rc = common_args(lors, n, lor_stride, image, image_strides, image_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
+    if (n > 0 && !out) return fail(SRF_EINVAL, "out must not be NULL");
+    TofParams tp{0, 0, 0};
+    return launch_trace<false, RULES_PROJ, GATHER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, nullptr, out, (cudaStream_t)stream);
+}
+
+int srf_backprojection(const float *lors, int64_t n, int32_t lor_stride, const float *values,
+                       float *image, const int64_t image_strides[3], float *image_t,
+                       const int64_t image_t_strides[3], const int32_t grid[3],
+                       const float center[3], const float size[3], void *stream) {
+    Grid g; View v, vt; int rc;
+    if ((rc = common_args(lors, n, lor_stride, image, image_strides, image_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
+    if (n > 0 && !values) return fail(SRF_EINVAL, "values must not be NULL");
+    TofParams tp{0, 0, 0};
+    return launch_trace<false, RULES_BACK, SCATTER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
+}
+
+int srf_projection_tof(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
+                       int32_t tof_stride, float tof_bin, float tof_sigma2, float tof_nsigma,
+                       const float *image, const int64_t image_strides[3], const float *image_t,
+                       const int64_t image_t_strides[3], const int32_t grid[3],
+                       const float center[3], const float size[3], float *out, void *stream) {
+    Grid g; View v, vt; TofParams tp; int rc;
+    if ((rc = common_args(lors, n, lor_stride, image, image_strides, image_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
+    if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
+    if (n > 0 && !out) return fail(SRF_EINVAL, "out must not be NULL");
+    return launch_trace<true, RULES_PROJ, GATHER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, nullptr, out, (cudaStream_t)stream);
+}
+
+int srf_backprojection_tof(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
+                           int32_t tof_stride, float tof_bin, float tof_sigma2, float tof_nsigma,
+                           const float *values, float *image, const int64_t image_strides[3],
+                           float *image_t, const int64_t image_t_strides[3],
+                           const int32_t grid[3], const float center[3], const float size[3],
+                           void *stream) {
+    Grid g; View v, vt; TofParams tp; int rc;
+    if ((rc = common_args(lors, n, lor_stride, image, image_strides, image_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
+    if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
+    if (n > 0 && !values) return fail(SRF_EINVAL, "values must not be NULL");
+    return launch_trace<true, RULES_BACK, SCATTER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
+}
+
+int srf_projection_adjoint(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
+                           int32_t tof_stride, float tof_bin, float tof_sigma2, float tof_nsigma,
+                           const float *values, float *image, const int64_t image_strides[3],
+                           float *image_t, const int64_t image_t_strides[3],
+                           const int32_t grid[3], const float center[3], const float size[3],
+                           void *stream) {
+    Grid g; View v, vt; int rc;
+    if ((rc = common_args(lors, n, lor_stride, image, image_strides, image_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
+    if (n > 0 && !values) return fail(SRF_EINVAL, "values must not be NULL");
+    if (tof) {
+        TofParams tp;
+        if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
+        return launch_trace<true, RULES_PROJ, SCATTER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
+    }
+    TofParams tp{0, 0, 0};
+    return launch_trace<false, RULES_PROJ, SCATTER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
+}
+
+int srf_count_pairs(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
+                    int32_t tof_stride, float tof_bin, float tof_sigma2, float tof_nsigma,
+                    int32_t rules, const int32_t grid[3], const float center[3],
+                    const float size[3], unsigned long long *count, void *stream) {
+    Grid g; int rc;
+    if ((rc = check_lors(lors, n, lor_stride))) return rc;
+    if ((rc = check_geometry(grid, center, size, g))) return rc;
+    if (!count) return fail(SRF_EINVAL, "count must not be NULL");
+    if (rules != RULES_PROJ && rules != RULES_BACK) return fail(SRF_EINVAL, "unknown rules %d", rules);
+    const int64_t st[3] = {1, g.nx, (int64_t)g.nx * g.ny};
+    View v{nullptr, {st[0], st[1], st[2]}}, vt{nullptr, {0, 0, 0}};
+    float *out = (float *)count;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (tof) {
+        TofParams tp;
+        if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
+        return rules == RULES_PROJ
+                   ? launch_trace<true, RULES_PROJ, COUNT>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, nullptr, out, s)
+                   : launch_trace<true, RULES_BACK, COUNT>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, nullptr, out, s);
+    }
+    TofParams tp{0, 0, 0};
+    return rules == RULES_PROJ
+               ? launch_trace<false, RULES_PROJ, COUNT>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, nullptr, out, s)
+               : launch_trace<false, RULES_BACK, COUNT>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, nullptr, out, s);
+}
+
+static int elementwise_args(const void *dst, const int64_t *ds, const void *src, const int64_t *ss,
+                            const int32_t grid[3], Grid &g, View &d, View &sv) {
+    if (!grid) return fail(SRF_EINVAL, "grid must not be NULL");
+    const float c[3] = {0, 0, 0}, sz[3] = {1, 1, 1};
+    int rc;
+    if ((rc = check_geometry(grid, c, sz, g))) return rc;
+    if ((rc = check_view(dst, ds, g, "dst", d, true))) return rc;
+    if ((rc = check_view(src, ss, g, "src", sv, true))) return rc;
+    return SRF_OK;
+}
+
+int srf_fold_views(float *dst, const int64_t dst_strides[3], const float *src,
+                   const int64_t src_strides[3], const int32_t grid[3], void *stream) {
+    Grid g; View d, sv; int rc;
+    if ((rc = elementwise_args(dst, dst_strides, src, src_strides, grid, g, d, sv))) return rc;
+    const int64_t total = (int64_t)g.nx * g.ny * g.nz;
+    unsigned blocks = grid_for(k_fold, total, kBlock);
+    k_fold<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(dst, d, src, sv, g.nx, g.ny, g.nz);
+    return check_cuda("fold kernel launch");
+}
+
+int srf_copy_view(float *dst, const int64_t dst_strides[3], const float *src,
+                  const int64_t src_strides[3], const int32_t grid[3], void *stream) {
+    Grid g; View d, sv; int rc;
+    if ((rc = elementwise_args(dst, dst_strides, src, src_strides, grid, g, d, sv))) return rc;
+    const int64_t total = (int64_t)g.nx * g.ny * g.nz;
+    unsigned blocks = grid_for(k_copy, total, kBlock);
+    k_copy<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(dst, d, src, sv, g.nx, g.ny, g.nz);
+    return check_cuda("copy kernel launch");
+}
+
+}  // extern "C"

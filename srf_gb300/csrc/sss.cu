@@ -1,0 +1,162 @@
+// Single-scatter simulation core on the GPU.
+//
+// Follows srfnef/corrections/scattering/scatter_fraction/scatter_fraction.py:40-136 and
+// kn_formula.py:6-46 (numba.cuda kernels loop_all_lors/loop_all_s in the reference):
+//   for LOR pair (A, B) and scatter point S:
+//     theta  = whole degrees of acos(-(|AS|^2 + |SB|^2 - |AB|^2) / (2 |AS| |SB|)), in radians
+//     E'     = 511 / (2 - cos theta)
+//     Ia     = atten_SA * atten_SB^(511/E') * em_SA ;  Ib = atten_SA^(511/E') * atten_SB * em_SB
+//     term   = area(S->A) * eff(E') * area(S->B) * fkn(theta) * mu(S) * (Ia + Ib) / |SA|^2 / |SB|^2
+//   scatter = sum_S term ;  scale = (|AB| / area(A->B))^2
+// with area(P->Q) = ((Q - P) . n_Q) / |PQ|, n_Q the normal of Q's block (get_block_theta),
+// eff(E) = sum_{e = low, low+5, .. < high} exp(-(e - E)^2 / (2 res^2)), res = sqrt(511)*resolution,
+// and fkn's Klein-Nishina factor evaluated at the angle (the reference passes theta where the
+// formula expects cos theta; kn_formula.py:11).
+//
+// GB300 design: because theta is quantised to whole degrees, cos theta, 511/E', eff(E') and the
+// Klein-Nishina factor take at most 181 values; each block builds those tables in shared memory
+// (double precision, then rounded) and the inner loop is table lookups plus two power
+// functions. One warp per LOR pair, lanes over scatter points, so the crystal-major emission and
+// attenuation rows are read coalesced. The angle is evaluated in FP32 and re-evaluated in FP64
+// when it falls within 0.01 degree of a whole degree or |cos| > 0.999, so its quantisation
+// agrees with a double-precision evaluation.
+#include "common.cuh"
+
+namespace srf {
+
+constexpr int kAngles = 181;
+
+__device__ __forceinline__ double block_theta_d(int ncpr, int nbpr, int gb1, double px, double py, double pz) {
+    const double norm = sqrt(px * px + py * py + pz * pz);
+    double th = acos(px / norm) / M_PI * 180.0;
+    if (py < 0) th = 360.0 - th;
+    double fixed = fmod(th + 180.0 / ncpr * gb1, 360.0);
+    if (fixed < 0) fixed += 360.0;
+    const double id_block = floor(fixed / 360.0 * nbpr);
+    return id_block / nbpr * 2.0 * M_PI;
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, const float *__restrict__ cpos,
+      const float *__restrict__ spos, int n_s, const float *__restrict__ em,
+      const float *__restrict__ at, const float *__restrict__ umap, int u0, int u1, int u2,
+      float us0, float us1, float us2, int ncpr, int nbpr, int gb1, int low, int high, double res,
+      float *__restrict__ scatter, float *__restrict__ scale) {
+    __shared__ float t_g[kAngles], t_eff[kAngles], t_fk[kAngles];
+    for (int t = threadIdx.x; t < kAngles; t += blockDim.x) {
+        const double ang = (double)t / 180.0 * M_PI;
+        const double c = cos(ang);
+        const double e_sc = 511.0 / (2.0 - c);
+        double eff = 0.0;
+        for (int e = low; e < high; e += 5) eff += exp(-((double)e - e_sc) * ((double)e - e_sc) / 2.0 / (res * res));
+        const double a = ang;  // the reference's fkn receives the angle
+        const double diff = 1.0 / ((2.0 - a) * (2.0 - a)) * ((1.0 + a * a) / 2.0 + (1.0 - a) * (1.0 - a) / 2.0 / (2.0 - a));
+        const double sigma = M_PI * (40.0 / 9.0 - 3.0 * log(3.0));
+        t_g[t] = (float)(511.0 / e_sc);
+        t_eff[t] = (float)eff;
+        t_fk[t] = (float)(diff / sigma);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t k = warp; k < n_pairs; k += nwarps) {
+        const int a = __ldg(pairs + 2 * k), b = __ldg(pairs + 2 * k + 1);
+        const float ax = __ldg(cpos + 3 * a), ay = __ldg(cpos + 3 * a + 1), az = __ldg(cpos + 3 * a + 2);
+        const float bx = __ldg(cpos + 3 * b), by = __ldg(cpos + 3 * b + 1), bz = __ldg(cpos + 3 * b + 2);
+        const double tha = block_theta_d(ncpr, nbpr, gb1, ax, ay, az);
+        const double thb = block_theta_d(ncpr, nbpr, gb1, bx, by, bz);
+        const float nax = (float)cos(tha), nay = (float)sin(tha);
+        const float nbx = (float)cos(thb), nby = (float)sin(thb);
+        const float dabx = bx - ax, daby = by - ay, dabz = bz - az;
+        const float ab2 = dabx * dabx + daby * daby + dabz * dabz;
+        const float ab = sqrtf(ab2);
+        const float *ema = em + (int64_t)a * n_s, *emb = em + (int64_t)b * n_s;
+        const float *ata = at + (int64_t)a * n_s, *atb = at + (int64_t)b * n_s;
+        float acc = 0.0f;
+        for (int s = lane; s < n_s; s += 32) {
+            const float sx = __ldg(spos + 3 * s), sy = __ldg(spos + 3 * s + 1), sz = __ldg(spos + 3 * s + 2);
+            const float dax = ax - sx, day = ay - sy, daz = az - sz;
+            const float dbx = bx - sx, dby = by - sy, dbz = bz - sz;
+            const float as2 = dax * dax + day * day + daz * daz;
+            const float sb2 = dbx * dbx + dby * dby + dbz * dbz;
+            const float as = sqrtf(as2), sb = sqrtf(sb2);
+            float arg = -(as2 + sb2 - ab2) / (2.0f * as * sb);
+            arg = fminf(1.0f, fmaxf(-1.0f, arg));
+            float deg = acosf(arg) * (float)(180.0 / M_PI);
+            const float fr = deg - floorf(deg);
+            int ti;
+            if (fr < 0.01f || fr > 0.99f || fabsf(arg) > 0.999f) {
+                const double Dax = (double)ax - sx, Day = (double)ay - sy, Daz = (double)az - sz;
+                const double Dbx = (double)bx - sx, Dby = (double)by - sy, Dbz = (double)bz - sz;
+                const double Dab = sqrt((double)dabx * dabx + (double)daby * daby + (double)dabz * dabz);
+                const double Das = sqrt(Dax * Dax + Day * Day + Daz * Daz);
+                const double Dsb = sqrt(Dbx * Dbx + Dby * Dby + Dbz * Dbz);
+                double dargs = -(Das * Das + Dsb * Dsb - Dab * Dab) / (2 * Das * Dsb);
+                dargs = fmin(1.0, fmax(-1.0, dargs));
+                ti = (int)(acos(dargs) / M_PI * 180.0);
+            } else {
+                ti = (int)deg;
+            }
+            ti = min(max(ti, 0), kAngles - 1);
+            // mu at the nearest voxel of S (kn_formula.py:12-14); outside the map counts as 0
+            const int g0 = (int)((sx / us0 + 0.5f) * u0);
+            const int g1 = (int)((sy / us1 + 0.5f) * u1);
+            const int g2 = (int)((sz / us2 + 0.5f) * u2);
+            float mu = 0.0f;
+            if (g0 >= 0 && g0 < u0 && g1 >= 0 && g1 < u1 && g2 >= 0 && g2 < u2)
+                mu = __ldg(umap + ((int64_t)g0 * u1 + g1) * u2 + g2);
+            const float gexp = t_g[ti];
+            const float a_a = __ldg(ata + s), a_b = __ldg(atb + s);
+            const float Ia = a_a * exp2f(__log2f(a_b) * gexp) * __ldg(ema + s);
+            const float Ib = exp2f(__log2f(a_a) * gexp) * a_b * __ldg(emb + s);
+            // area(S->A) uses A's block normal, area(S->B) B's
+            const float pa = (dax * nax + day * nay) / as;
+            const float pb = (dbx * nbx + dby * nby) / sb;
+            acc += pa * t_eff[ti] * pb * (t_fk[ti] * mu) * (Ia + Ib) / as2 / sb2;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            scatter[k] = acc;
+            const float area = (dabx * nbx + daby * nby) / ab;
+            const float q = ab / area;
+            scale[k] = q * q;
+        }
+    }
+}
+
+}  // namespace srf
+
+using namespace srf;
+
+extern "C" int srf_sss(const int32_t *pairs, int64_t n_pairs, const float *crystal_pos,
+                       int32_t n_crystals, const float *scatter_pos, int32_t n_scatter,
+                       const float *sumup_emission, const float *atten, const float *umap,
+                       const int32_t umap_shape[3], const float umap_size[3],
+                       int32_t nb_crystals_per_ring, int32_t nb_blocks_per_ring,
+                       const int32_t grid_block[3], int32_t low_energy, int32_t high_energy,
+                       float resolution, float *scatter, float *scale, void *stream) {
+    if (n_pairs < 0 || n_crystals <= 0 || n_scatter < 0) return fail(SRF_EINVAL, "bad counts");
+    if (n_pairs == 0) return ok();
+    if (!pairs || !crystal_pos || !scatter || !scale || !umap_shape || !umap_size || !grid_block)
+        return fail(SRF_EINVAL, "NULL argument");
+    if (n_scatter > 0 && (!scatter_pos || !sumup_emission || !atten || !umap))
+        return fail(SRF_EINVAL, "NULL scatter-point argument");
+    if (nb_crystals_per_ring <= 0 || nb_blocks_per_ring <= 0)
+        return fail(SRF_EINVAL, "ring counts must be positive");
+    for (int k = 0; k < 3; ++k) {
+        if (umap_shape[k] <= 0) return fail(SRF_EGRID, "umap_shape[%d] must be positive", k);
+        if (!std::isfinite(umap_size[k]) || !(umap_size[k] > 0)) return fail(SRF_EGRID, "umap_size[%d] must be > 0", k);
+    }
+    if (!std::isfinite(resolution) || !(resolution > 0)) return fail(SRF_ENONFINITE, "resolution must be > 0");
+    if (high_energy - low_energy > 5 * 100000) return fail(SRF_ERANGE, "energy window too wide");
+    const double res = sqrt(511.0) * (double)resolution;
+    unsigned blocks = grid_for(k_sss, n_pairs, kBlock / 32);
+    k_sss<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(
+        pairs, n_pairs, crystal_pos, scatter_pos, n_scatter, sumup_emission, atten, umap,
+        umap_shape[0], umap_shape[1], umap_shape[2], umap_size[0], umap_size[1], umap_size[2],
+        nb_crystals_per_ring, nb_blocks_per_ring, grid_block[1], low_energy, high_energy, res,
+        scatter, scale);
+    return check_cuda("sss kernel launch");
+}

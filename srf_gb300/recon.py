@@ -1,0 +1,232 @@
+"""List-mode MLEM / OSEM with srfnef's call signatures, each iteration a fused GPU subset step.
+
+* ``Mlem(n_iter, emap)(listmode)``                          srfnef/functions/mlem.py:23-45
+* ``MlemFull(n_iter, image_config, scanner, listmode, atten_corr, scatter_corr, psf_corr, emap)()``
+                                                             srfnef/functions/mlem_full.py:28-99
+* ``MlemFullTof(...)()``                                     srfnef/functions/mlem_full_tof.py:28-99
+* ``OsemFull(n_iter, n_sub, image_config, scanner, listmode, atten_corr, scatter_corr, norm_corr,
+  psf_corr, emap, image)()``                                 srfnef/functions/osem_full.py:30-87
+* ``OsemFullTof`` -- not in the reference (it has no TOF OSEM): OsemFull's subset loop with
+  MlemFullTof's update rule, cyclic subsets of a seeded permutation and an emap scaled per subset.
+
+Update rules, as the reference (float32 throughout):
+  Mlem        r = y / (p + mean(y)*1e-8)       emap zeros -> 1e8
+  MlemFull    r = div_no_nan(y, p)             emap zeros -> 1e8
+  MlemFullTof r = div_no_nan(y, p + 1e-5)      emap zeros -> 1e8
+  OsemFull    r = y / (p + 1e-8)               emap as given; subset i_iter // n_sub
+  x <- x * bp / emap
+``OsemFull.subset_rule='reference'`` keeps the reference's ``i_iter // n_sub`` (osem_full.py:68);
+'cyclic' uses ``i_iter % n_sub``. ``OsemFull.seed=None`` shuffles with numpy's global generator
+like the reference (osem_full.py:63-64); an int seeds a private generator.
+
+Each subset step is one ``srf_osem_subset`` launch (projection, ratio and backprojection per LOR)
+followed by one ``srf_osem_update`` launch.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import Any, Callable, Optional
+
+import numpy as np
+import torch
+
+from . import kernels
+from ._lib import SRF_RATIO_DIV_NO_NAN, SRF_RATIO_PLAIN
+from .data import Emap, Image, Listmode, _NefLike
+from .emap_generator import EmapGenerator
+from .functions import device, to_dev
+from .geometry import ImageConfig, PetEcatListmodeTrans, PetEcatScanner
+
+
+def _emap_dev(emap) -> torch.Tensor:
+    return kernels.xfast(to_dev(emap.data))
+
+
+def _result(state: kernels.SubsetState, like, center, size) -> Image:
+    x = state.x.contiguous()
+    if not isinstance(like, torch.Tensor):
+        x = x.cpu().numpy()
+    return Image(x, list(center), list(size))
+
+
+def _run_mlem(n_iter, lors_np_or_t, y, emap, shape, center, size, *, tof, rule, eps, guard,
+              tof_nsigma=0.0) -> kernels.SubsetState:
+    dev = device()
+    lors = to_dev(lors_np_or_t).contiguous()
+    yd = to_dev(y).contiguous()
+    em = _emap_dev(emap)
+    st = kernels.SubsetState(shape, center, size, dev)
+    for _ in range(n_iter):
+        st.subset(lors, yd, rule=rule, eps=eps, tof=tof, tof_nsigma=tof_nsigma)
+        st.update(em, guard_zero=guard)
+    return st
+
+
+@dataclasses.dataclass(frozen=True)
+class Mlem(_NefLike):
+    n_iter: Optional[int] = None
+    emap: Optional[Emap] = None
+
+    def __call__(self, listmode: Listmode) -> Image:
+        y = np.asarray(listmode.data.cpu() if isinstance(listmode.data, torch.Tensor) else listmode.data,
+                       dtype=np.float32)
+        eps = float(np.float32(np.mean(y) * 1e-8))
+        st = _run_mlem(self.n_iter, listmode.lors.data, listmode.data, self.emap, self.emap.shape,
+                       self.emap.center, self.emap.size, tof=None, rule=SRF_RATIO_PLAIN, eps=eps,
+                       guard=True)
+        return _result(st, self.emap.data, self.emap.center, self.emap.size)
+
+
+@dataclasses.dataclass(frozen=True)
+class MlemFull(_NefLike):
+    n_iter: Optional[int] = None
+    image_config: Optional[ImageConfig] = None
+    scanner: Optional[PetEcatScanner] = None
+    listmode: Optional[Listmode] = None
+    atten_corr: Any = None
+    scatter_corr: Any = None
+    psf_corr: Optional[Callable] = None
+    emap: Optional[Emap] = None
+
+    _tof = False
+    _eps = 0.0
+
+    def generate_emap(self) -> None:
+        object.__setattr__(self, "emap", EmapGenerator("block-full", self.scanner)(self.image_config))
+
+    def _tof_args(self):
+        return None
+
+    def _recon(self, listmode_) -> Image:
+        ic = self.image_config
+        st = _run_mlem(self.n_iter, self.listmode.lors.data, listmode_.data, self.emap, ic.shape,
+                       ic.center, ic.size, tof=self._tof_args(), rule=SRF_RATIO_DIV_NO_NAN,
+                       eps=self._eps, guard=True)
+        return _result(st, self.listmode.data, ic.center, ic.size)
+
+    def __call__(self) -> Image:
+        if self.emap is None:
+            self.generate_emap()
+        listmode_ = self.atten_corr(self.listmode) if self.atten_corr is not None else self.listmode
+        x = self._recon(listmode_)
+        x = self._after(x)
+        return self.psf_corr(x) if self.psf_corr is not None else x
+
+    def _after(self, x: Image) -> Image:
+        return x
+
+
+@dataclasses.dataclass(frozen=True)
+class MlemFullTof(MlemFull):
+    _tof = True
+    _eps = 1e-5
+
+    def _tof_args(self):
+        return (self.scanner.tof.tof_bin, self.scanner.tof.tof_sigma2)
+
+    def _after(self, x: Image) -> Image:
+        # mlem_full_tof.py:71-92: with a scatter correction, rerun on the corrected list mode
+        if self.scatter_corr is None:
+            return x
+        assert self.atten_corr is not None
+        listmode_ = self.scatter_corr(x, self.atten_corr.u_map, self.scanner, self.listmode)
+        return self._recon(listmode_)
+
+
+@dataclasses.dataclass(frozen=True)
+class OsemFull(_NefLike):
+    n_iter: Optional[int] = None
+    n_sub: Optional[int] = None
+    image_config: Optional[ImageConfig] = None
+    scanner: Optional[PetEcatScanner] = None
+    listmode: Optional[Listmode] = None
+    atten_corr: Any = None
+    scatter_corr: Any = None
+    norm_corr: Optional[bool] = None
+    psf_corr: Optional[Callable] = None
+    emap: Optional[Emap] = None
+    image: Optional[Image] = None
+    subset_rule: str = "reference"
+    seed: Optional[int] = None
+
+    def generate_emap(self) -> None:
+        # osem_full.py:45-47 asks for mode 'ring', which EcatEmapGenerator does not implement
+        object.__setattr__(self, "emap", EmapGenerator("ring", self.scanner)(self.image_config))
+
+    def __call__(self) -> Image:
+        if self.emap is None:
+            self.generate_emap()
+        listmode_ = PetEcatListmodeTrans(self.scanner)(self.listmode)
+        if self.atten_corr is not None:
+            listmode_ = self.atten_corr(listmode_)
+        ic = self.image_config
+        n = len(self.listmode)
+        rand_inds = np.arange(n)
+        if self.seed is None:
+            np.random.shuffle(rand_inds)
+        else:
+            rand_inds = np.random.default_rng(self.seed).permutation(n)
+        n_per_sub = n // self.n_sub
+        dev = device()
+        lors_all = to_dev(np.asarray(self.listmode.lors.data)[rand_inds]).contiguous()
+        y_all = to_dev(np.asarray(listmode_.data)[rand_inds]).contiguous()
+        em = _emap_dev(self.emap)
+        st = kernels.SubsetState(ic.shape, ic.center, ic.size, dev)
+        for i_iter in range(self.n_iter):
+            ind = i_iter // self.n_sub if self.subset_rule == "reference" else i_iter % self.n_sub
+            lo, hi = min(ind * n_per_sub, n), min((ind + 1) * n_per_sub, n)
+            st.subset(lors_all[lo:hi], y_all[lo:hi], rule=SRF_RATIO_PLAIN, eps=1e-8)
+            st.update(em, guard_zero=False)
+        x = _result(st, self.listmode.data, ic.center, ic.size)
+        return self.psf_corr(x) if self.psf_corr is not None else x
+
+
+@dataclasses.dataclass(frozen=True)
+class OsemFullTof(_NefLike):
+    """TOF list-mode OSEM: ``n_iter`` full passes of ``n_sub`` subsets each."""
+    n_iter: Optional[int] = None
+    n_sub: Optional[int] = None
+    image_config: Optional[ImageConfig] = None
+    scanner: Optional[PetEcatScanner] = None
+    listmode: Optional[Listmode] = None
+    emap: Optional[Emap] = None
+    tof_nsigma: float = 0.0
+    emap_scale: Optional[float] = None   # default 1 / n_sub
+    seed: int = 0
+    snap: bool = False
+
+    def prepare(self):
+        """Device-resident inputs: LORs and values permuted into subset order once."""
+        lm = PetEcatListmodeTrans(self.scanner)(self.listmode) if self.snap else self.listmode
+        dev = device()
+        n = len(lm)
+        lors = to_dev(lm.lors.data)
+        y = to_dev(lm.data)
+        perm = torch.as_tensor(np.random.default_rng(self.seed).permutation(n), device=dev)
+        lors = lors.index_select(0, perm).contiguous()
+        y = y.index_select(0, perm).contiguous()
+        scale = (1.0 / self.n_sub) if self.emap_scale is None else self.emap_scale
+        em = (_emap_dev(self.emap) * scale)
+        return lors, y, em
+
+    def run(self, lors: torch.Tensor, y: Optional[torch.Tensor], em: torch.Tensor,
+            state: Optional[kernels.SubsetState] = None, n_iter: Optional[int] = None,
+            track_loglik: bool = False) -> kernels.SubsetState:
+        ic = self.image_config
+        st = state or kernels.SubsetState(ic.shape, ic.center, ic.size, lors.device)
+        n = lors.shape[0]
+        n_per = n // self.n_sub
+        tof = (self.scanner.tof.tof_bin, self.scanner.tof.tof_sigma2)
+        for _ in range(self.n_iter if n_iter is None else n_iter):
+            for k in range(self.n_sub):
+                sl = slice(k * n_per, (k + 1) * n_per)
+                st.subset(lors[sl], None if y is None else y[sl], rule=SRF_RATIO_DIV_NO_NAN,
+                          eps=1e-5, tof=tof, tof_nsigma=self.tof_nsigma, track_loglik=track_loglik)
+                st.update(em, guard_zero=True)
+        return st
+
+    def __call__(self) -> Image:
+        lors, y, em = self.prepare()
+        st = self.run(lors, y, em)
+        ic = self.image_config
+        return _result(st, self.listmode.data, ic.center, ic.size)
