@@ -37,7 +37,7 @@ __device__ __forceinline__ double block_theta_d(int ncpr, int nbpr, int gb1, dou
 }
 
 __global__ void __launch_bounds__(kBlock)
-k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, const float *__restrict__ cpos,
+k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const float *__restrict__ cpos,
       const float *__restrict__ spos, int n_s, const float *__restrict__ em,
       const float *__restrict__ at, const float *__restrict__ umap, int u0, int u1, int u2,
       float us0, float us1, float us2, int ncpr, int nbpr, int gb1, int low, int high, double res,
@@ -62,6 +62,10 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, const float *__restric
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t k = warp; k < n_pairs; k += nwarps) {
         const int a = __ldg(pairs + 2 * k), b = __ldg(pairs + 2 * k + 1);
+        if (a < 0 || a >= n_crystals || b < 0 || b >= n_crystals) {  // invalid id: no contribution
+            if (lane == 0) { scatter[k] = 0.0f; scale[k] = 0.0f; }
+            continue;
+        }
         const float ax = __ldg(cpos + 3 * a), ay = __ldg(cpos + 3 * a + 1), az = __ldg(cpos + 3 * a + 2);
         const float bx = __ldg(cpos + 3 * b), by = __ldg(cpos + 3 * b + 1), bz = __ldg(cpos + 3 * b + 2);
         const double tha = block_theta_d(ncpr, nbpr, gb1, ax, ay, az);
@@ -154,7 +158,7 @@ extern "C" int srf_sss(const int32_t *pairs, int64_t n_pairs, const float *cryst
     const double res = sqrt(511.0) * (double)resolution;
     unsigned blocks = grid_for(k_sss, n_pairs, kBlock / 32);
     k_sss<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(
-        pairs, n_pairs, crystal_pos, scatter_pos, n_scatter, sumup_emission, atten, umap,
+        pairs, n_pairs, n_crystals, crystal_pos, scatter_pos, n_scatter, sumup_emission, atten, umap,
         umap_shape[0], umap_shape[1], umap_shape[2], umap_size[0], umap_size[1], umap_size[2],
         nb_crystals_per_ring, nb_blocks_per_ring, grid_block[1], low_energy, high_energy, res,
         scatter, scale);
