@@ -317,3 +317,62 @@ def rel_l2(a, b) -> float:
     b = np.asarray(b, dtype=np.float64)
     den = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
+
+
+# ---------------------------------------------------------------- scatter correction pipeline
+
+def umap_project(umap, lors):
+    """UmapProject (attenuation_correct.py:31-40) over the oracle projector."""
+    lors = np.ascontiguousarray(lors, dtype=np.float32)
+    p = projection(umap.data, np.ascontiguousarray(lors[:, :6]), umap.shape, umap.center, umap.size)
+    L = np.sqrt((lors[:, 0] - lors[:, 3]) ** 2 + (lors[:, 1] - lors[:, 4]) ** 2 + (lors[:, 2] - lors[:, 5]) ** 2)
+    return np.exp(-(p * L * L / umap.unit_size[0]))
+
+
+def scatter_preprocess(scanner, listmode, emission, umap):
+    """scatter.py:57-73 / preprocess.py:6-75 with every projection done by the oracle. The numpy
+    helpers for sinogram bins and scatter points come from srf_gb300.scatter (checked against the
+    reference's own host code by tests/test_host_logic.py)."""
+    from srf_gb300 import scatter as S
+    lors = S.get_all_lors_id(scanner.nb_crystals)
+    sinogram = S.lm2sino(listmode, scanner)
+    index = np.where(sinogram > 0)[0].astype(np.int32)
+    scat = S.pre_all_scatter_position(emission)
+    cryst = S.get_all_crystal_position(scanner)
+    L = S.get_lors(cryst, scat).data
+    em = projection(emission.data, np.ascontiguousarray(L[:, :6]), emission.shape, emission.center,
+                    emission.size)
+    len2 = (L[:, 3] - L[:, 0]) ** 2 + (L[:, 4] - L[:, 1]) ** 2 + (L[:, 5] - L[:, 2]) ** 2
+    atten = umap_project(umap, L)
+    p1, p2 = cryst[lors[index, 0]], cryst[lors[index, 1]]
+    lors7 = np.hstack((p1, p2, np.ones((p1.shape[0], 1), np.float32))).astype(np.float32)
+    atten_lors = umap_project(umap * 1.3, lors7).reshape(-1, 1)
+    return dict(lors=lors, sinogram=sinogram, index=index, scatter_position=scat,
+                crystal_position=cryst, sumup_emission=em * len2, atten=atten,
+                atten_lors=atten_lors)
+
+
+def scatter_correct(corr, emission, umap, scanner, pre):
+    """ScatterCorrect.__call__ (scatter.py:25-55) with the oracle's SSS sums."""
+    import sys as _sys
+    from srf_gb300 import scatter as S
+    from srf_gb300.data import Listmode, Lors
+    index = pre["index"]
+    ns = pre["scatter_position"].shape[0]
+    nc = pre["crystal_position"].shape[0]
+    grid_block = np.array(scanner.blocks.shape, dtype=np.int32)
+    size_block = np.array(scanner.blocks.size, dtype=np.float32)
+    raw, scale = sss(pre["lors"][index, :2], pre["crystal_position"], pre["scatter_position"],
+                     pre["sumup_emission"].reshape(nc, ns), pre["atten"].reshape(nc, ns),
+                     umap.data, umap.size, scanner.nb_blocks_per_ring * scanner.blocks.shape[1],
+                     scanner.nb_blocks_per_ring, grid_block, int(corr.low_energy),
+                     int(corr.high_energy), float(corr.resolution))
+    frac, scl = S.scatter_scaling(raw.reshape(-1, 1), scale.reshape(-1, 1), int(corr.low_energy),
+                                  int(corr.high_energy), float(corr.resolution), grid_block,
+                                  size_block)
+    sino = pre["sinogram"]
+    out = np.zeros_like(sino)
+    out[index] = (sino[index] - frac / np.sum(frac) * np.sum(sino[index]) * corr.scatter_fraction) \
+        * scl / (pre["atten_lors"] + _sys.float_info.min)
+    data = S.sino2lm(scanner, out, pre["lors"])
+    return Listmode(data[:, 6].astype(np.float32), Lors(data.astype(np.float32)))

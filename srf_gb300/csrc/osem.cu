@@ -8,62 +8,168 @@
 // accumulator, applies x*bp/emap, refreshes the y-fastest copy of x and zeroes both
 // accumulators in one pass over the image.
 #include "common.cuh"
+#include "fused.cuh"
 
 namespace srf {
 
+constexpr int kUnroll = 4;  // slabs per lane per chunk
+
+// Generic path for a LOR whose projector and backprojector traverse along different axes
+// (non-TOF with |xd| == |yd|): two setups, as in the standalone kernels.
 template <int G, bool TOF>
-__global__ void __launch_bounds__(kBlock)
+__device__ __forceinline__ void tie_path(const float *l, float tv, float yv, int lane, const Grid &g,
+                                         const TofParams &tp, const View &x, const View &xt,
+                                         const View &bp, const View &bpt, int rule, float eps,
+                                         double &ll, bool want_ll) {
+    float acc = 0.0f;
+    LorSetup S;
+    if (setup_lor<TOF, RULES_PROJ>(l[0], l[1], l[2], l[3], l[4], l[5], tv, g, tp, x.st, xt.st, xt.ptr != nullptr, S)) {
+        const float *im = (!S.xdom && xt.ptr) ? xt.ptr : x.ptr;
+        for (int ip = S.lo + lane; ip <= S.hi; ip += G)
+            slab<TOF, RULES_PROJ>(S, ip, [&](int32_t off, float w) { acc += __ldg(im + off) * w; });
+    }
+    const float p = group_sum<G>(acc);
+    const float den = __fadd_rn(p, eps);
+    const float r = (rule == SRF_RATIO_DIV_NO_NAN) ? ((den == 0.0f) ? 0.0f : __fdiv_rn(yv, den)) : __fdiv_rn(yv, den);
+    if (want_ll && lane == 0 && den > 0.0f) ll += (double)yv * (double)__logf(den);
+    if (r != 0.0f && setup_lor<TOF, RULES_BACK>(l[0], l[1], l[2], l[3], l[4], l[5], tv, g, tp, bp.st, bpt.st, bpt.ptr != nullptr, S)) {
+        float *im = (!S.xdom && bpt.ptr) ? bpt.ptr : bp.ptr;
+        for (int ip = S.lo + lane; ip <= S.hi; ip += G)
+            slab<TOF, RULES_BACK>(S, ip, [&](int32_t off, float w) { atomicAdd(im + off, r * w); });
+    }
+}
+
+// One warp handles 32 consecutive LORs per round: lane j sets up LOR j into shared memory, then
+// the warp's 32/G groups walk the records. x/x_t and bp/bp_t must have equal strides (offsets are
+// computed once for the gather and the scatter).
+template <int G, bool TOF>
+__global__ void __launch_bounds__(kBlock, 2)
 k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
               int tof_stride, Grid g, TofParams tp, const float *__restrict__ y, int rule, float eps,
               View x, View xt, View bp, View bpt, double *__restrict__ loglik) {
     constexpr int GPW = 32 / G;
+    __shared__ LorRec recs[kBlock / 32][32];
+    const int wib = threadIdx.x >> 5;
+    const int lane32 = threadIdx.x & 31;
     const int lane = threadIdx.x & (G - 1);
-    const int gi = (threadIdx.x & 31) / G;
+    const int gi = lane32 / G;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const bool have_xt = xt.ptr != nullptr, have_bpt = bpt.ptr != nullptr;
+    const GridK k = make_gridk<TOF>(g, tp);
+    const bool have_t = xt.ptr != nullptr;
+    const bool want_ll = loglik != nullptr;
     double ll = 0.0;
-    for (int64_t base = warp * GPW; base < n; base += nwarps * GPW) {
-        const int64_t i = base + gi;
-        const bool valid = i < n;
-        float x1 = 0, y1 = 0, z1 = 0, x2 = 0, y2 = 0, z2 = 0, tv = 0;
-        float acc = 0.0f;
-        if (valid) {
-            const float *l = lors + i * stride;
-            x1 = __ldg(l); y1 = __ldg(l + 1); z1 = __ldg(l + 2);
-            x2 = __ldg(l + 3); y2 = __ldg(l + 4); z2 = __ldg(l + 5);
-            if (TOF) tv = __ldg(tof + i * tof_stride);
-            LorSetup S;
-            if (setup_lor<TOF, RULES_PROJ>(x1, y1, z1, x2, y2, z2, tv, g, tp, x.st, xt.st, have_xt, S)) {
-                const float *im = (!S.xdom && have_xt) ? xt.ptr : x.ptr;
-                for (int ip = S.lo + lane; ip <= S.hi; ip += G)
-                    slab<TOF, RULES_PROJ>(S, ip, [&](int32_t off, float w) { acc += __ldg(im + off) * w; });
+    for (int64_t base = warp * 32; base < n; base += nwarps * 32) {
+        // lane-parallel setup of the warp's next 32 LORs
+        {
+            const int64_t i = base + lane32;
+            LorRec R;
+            if (i < n) {
+                const float *l = lors + i * stride;
+                float lv[6];
+#pragma unroll
+                for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
+                const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
+                const float yv = y ? __ldg(y + i) : 1.0f;
+                R = setup_rec<TOF>(lv, tv, yv, g, k);
+            } else {
+                R.flags = 0;
+                R.lo = 1;
+                R.hi = 0;
             }
+            recs[wib][lane32] = R;
         }
-        const float p = group_sum<G>(acc);
-        if (valid) {
-            const float yv = y ? __ldg(y + i) : 1.0f;
+        __syncwarp();
+        for (int j0 = 0; j0 < 32; j0 += GPW) {
+            const int j = j0 + gi;
+            const LorRec R = recs[wib][j];
+            const int64_t i = base + j;
+            if (R.flags & F_TIE) {
+                // rare: re-read the LOR and take the two-setup path
+                float lv[6];
+                const float *l = lors + i * stride;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
+                const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
+                tie_path<G, TOF>(lv, tv, R.yv, lane, g, tp, x, xt, bp, bpt, rule, eps, ll, want_ll);
+                continue;
+            }
+            const bool valid = R.flags & F_VALID;
+            const LorRun run = make_run(R, g, k, x.st, xt.st, have_t);
+            const float *xim = (!run.xdom && have_t) ? xt.ptr : x.ptr;
+            float *bim = (!run.xdom && have_t) ? bpt.ptr : bp.ptr;
+            const bool proj_ok = R.flags & F_PROJ;
+            const bool single = (run.hi - run.lo + 1) <= G * kUnroll;
+            int32_t o[kUnroll][3];
+            float w[kUnroll][3];
+            float acc = 0.0f;
+            if (valid) {
+                for (int c0 = run.lo; c0 <= run.hi; c0 += G * kUnroll) {
+                    bool pm[kUnroll];
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) {
+                        const int ip = c0 + lane + G * u;
+                        if (ip <= run.hi) {
+                            candidates<TOF>(run, k, ip, o[u], w[u], pm[u]);
+                        } else {
+                            o[u][0] = o[u][1] = o[u][2] = 0;
+                            w[u][0] = w[u][1] = w[u][2] = 0.0f;
+                            pm[u] = false;
+                        }
+                    }
+                    if (proj_ok) {
+                        float xv[kUnroll][3];
+#pragma unroll
+                        for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+                            for (int c = 0; c < 3; ++c)
+                                xv[u][c] = (pm[u] && w[u][c] != 0.0f) ? __ldg(xim + o[u][c]) : 0.0f;
+#pragma unroll
+                        for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) acc = fmaf(xv[u][c], w[u][c], acc);
+                    }
+                }
+            }
+            const float p = group_sum<G>(acc) * R.invL2;
+            if (!valid) continue;
             const float den = __fadd_rn(p, eps);
             float r;
             if (rule == SRF_RATIO_DIV_NO_NAN)
-                r = (den == 0.0f) ? 0.0f : __fdiv_rn(yv, den);
+                r = (den == 0.0f) ? 0.0f : __fdiv_rn(R.yv, den);
             else
-                r = __fdiv_rn(yv, den);
-            if (loglik && lane == 0 && den > 0.0f) ll += (double)yv * (double)__logf(den);
-            if (r != 0.0f) {
-                LorSetup S;
-                if (setup_lor<TOF, RULES_BACK>(x1, y1, z1, x2, y2, z2, tv, g, tp, bp.st, bpt.st, have_bpt, S)) {
-                    float *im = (!S.xdom && have_bpt) ? bpt.ptr : bp.ptr;
-                    for (int ip = S.lo + lane; ip <= S.hi; ip += G)
-                        slab<TOF, RULES_BACK>(S, ip, [&](int32_t off, float w) { atomicAdd(im + off, r * w); });
+                r = __fdiv_rn(R.yv, den);
+            if (want_ll && lane == 0 && den > 0.0f) ll += (double)R.yv * (double)__logf(den);
+            if (r == 0.0f) continue;
+            if (single) {
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                        if (w[u][c] != 0.0f) atomicAdd(bim + o[u][c], r * w[u][c]);
+            } else {
+                for (int c0 = run.lo; c0 <= run.hi; c0 += G * kUnroll) {
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) {
+                        const int ip = c0 + lane + G * u;
+                        if (ip > run.hi) break;
+                        int32_t oo[3];
+                        float ww[3];
+                        bool pmu;
+                        candidates<TOF>(run, k, ip, oo, ww, pmu);
+#pragma unroll
+                        for (int c = 0; c < 3; ++c)
+                            if (ww[c] != 0.0f) atomicAdd(bim + oo[c], r * ww[c]);
+                    }
                 }
             }
         }
+        __syncwarp();
     }
-    if (loglik) {
+    if (want_ll) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) ll += __shfl_xor_sync(0xffffffffu, ll, o);
-        if ((threadIdx.x & 31) == 0 && ll != 0.0) atomicAdd(loglik, ll);
+        for (int o2 = 16; o2 > 0; o2 >>= 1) ll += __shfl_xor_sync(0xffffffffu, ll, o2);
+        if (lane32 == 0 && ll != 0.0) atomicAdd(loglik, ll);
     }
 }
 
@@ -73,7 +179,7 @@ static int launch_osem_g(const float *lors, int64_t n, int stride, const float *
                          const View &x, const View &xt, const View &bp, const View &bpt,
                          double *loglik, cudaStream_t s) {
     auto kern = k_osem_subset<G, TOF>;
-    unsigned blocks = grid_for(kern, n, kBlock / G);
+    unsigned blocks = grid_for(kern, n, kBlock);
     kern<<<blocks, kBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik);
     return check_cuda("osem subset kernel launch");
 }
@@ -162,6 +268,7 @@ int srf_osem_subset(const float *lors, int64_t n, int32_t lor_stride, const floa
     if ((rc = check_view(x_t, ys, g, "x_t", vxt, false))) return rc;
     if ((rc = check_view(bp, xs, g, "bp", vbp, true))) return rc;
     if ((rc = check_view(bp_t, ys, g, "bp_t", vbpt, false))) return rc;
+    if ((x_t == nullptr) != (bp_t == nullptr)) return fail(SRF_EINVAL, "x_t and bp_t must both be given or both be NULL");
     if (n == 0) return ok();
     cudaStream_t s = (cudaStream_t)stream;
     if (tof) {

@@ -267,18 +267,20 @@ __device__ __forceinline__ void slab(const LorSetup &S, int ip, F &&visit) {
 #undef SRF_V
 }
 
-// Sum over a group of G lanes (G a power of two <= 32, groups aligned within the warp).
+// Lanes of this thread's group of G (G a power of two <= 32, groups aligned within the warp).
 template <int G>
-__device__ __forceinline__ float group_sum(float v) {
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
-    return v;
+__device__ __forceinline__ unsigned group_mask() {
+    if (G == 32) return 0xffffffffu;
+    return ((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1));
 }
 
+// Sum over a group of G lanes. Only the group's own lanes take part, so groups of one warp may
+// call it from different places.
 template <int G>
-__device__ __forceinline__ double group_sum_d(double v) {
+__device__ __forceinline__ float group_sum(float v) {
+    const unsigned m = group_mask<G>();
 #pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(m, v, o, G);
     return v;
 }
 

@@ -1,0 +1,107 @@
+"""GPU: differentiable projector (finite differences in FP64, adjoint identity) and the
+single-scatter simulation (kernel and full correction pipeline) against the CPU oracle."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("tof", [False, True])
+def test_projector_gradient_finite_differences(cuda_lib, small_case, tof):
+    """d/dx_v of sum(p - y log p) against central differences in FP64 on 64 voxels.
+    A is linear, so p(x +- h e_v) = p(x) +- h A e_v with A e_v the projection of a one-hot image."""
+    from srf_gb300 import autograd, kernels
+    ic, sc = small_case["ic"], small_case["scanner"]
+    t = (sc.tof.tof_bin, sc.tof.tof_sigma2) if tof else None
+    dev = torch.device("cuda", 0)
+    lors = torch.as_tensor(small_case["lors"], device=dev)
+    x0 = torch.as_tensor(small_case["act"] + 0.5, device=dev)
+    x = x0.clone().requires_grad_(True)
+    p = autograd.project(x, lors, ic.center, ic.size, tof=t)
+    y = torch.poisson(p.detach().clamp(min=0) * 50 + 1)
+    loss = autograd.poisson_nll(p, y, eps=1e-3)
+    loss.backward()
+    grad = x.grad.cpu().numpy().astype(np.float64)
+    p64 = p.detach().cpu().numpy().astype(np.float64)
+    y64 = y.cpu().numpy().astype(np.float64)
+    rng = np.random.default_rng(0)
+    flat = np.flatnonzero(np.abs(grad) > 1e-3 * np.abs(grad).max())
+    vox = rng.choice(flat, 64, replace=False)
+    h = 1e-3
+
+    def L(pp):
+        return float(np.sum(pp - y64 * np.log(pp + 1e-3)))
+    for v in vox:
+        e = torch.zeros(ic.shape, device=dev)
+        e.view(-1)[v] = 1.0
+        a = kernels.project(lors, e, ic.center, ic.size, tof=t).cpu().numpy().astype(np.float64)
+        fd = (L(p64 + h * a) - L(p64 - h * a)) / (2 * h)
+        g = grad.reshape(-1)[v]
+        assert abs(fd - g) <= 1e-4 * max(abs(fd), 1e-6 * np.abs(grad).max()), (v, fd, g)
+
+
+def test_batched_projector_adjoint_identity(cuda_lib, small_case):
+    from srf_gb300 import autograd
+    ic, sc = small_case["ic"], small_case["scanner"]
+    dev = torch.device("cuda", 0)
+    lors = torch.as_tensor(small_case["lors"], device=dev)
+    rng = np.random.default_rng(1)
+    xb = torch.as_tensor(rng.random((3, *ic.shape)).astype(np.float32), device=dev).requires_grad_(True)
+    t = (sc.tof.tof_bin, sc.tof.tof_sigma2)
+    p = autograd.project(xb, lors, ic.center, ic.size, tof=t)
+    assert p.shape == (3, lors.shape[0])
+    yv = torch.as_tensor(rng.random((3, lors.shape[0])).astype(np.float32), device=dev)
+    (p * yv).sum().backward()
+    lhs = float((p.detach().double() * yv.double()).sum())
+    rhs = float((xb.detach().double() * xb.grad.double()).sum())
+    assert abs(lhs - rhs) / abs(lhs) <= 1e-6
+
+
+def test_sss_kernel_matches_oracle(cuda_lib, oracle):
+    import os
+    from srf_gb300 import kernels
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "sss.npz")))
+    rng = np.random.default_rng(3)
+    n_c = g["crystal"].shape[0]
+    pairs = np.vstack([g["pairs"], rng.integers(0, n_c, size=(3000, 2))]).astype(np.int32)
+    pairs = pairs[pairs[:, 0] != pairs[:, 1]]
+    ref_s, ref_c = oracle.sss(pairs, g["crystal"], g["scatter"], g["sumup"], g["atten"], g["umap"],
+                              g["usize"], int(g["ncpr"]), int(g["nbpr"]), g["grid_block"],
+                              int(g["low"]), int(g["high"]), float(g["res"]))
+    dev = torch.device("cuda", 0)
+    d = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to(dev)
+    sc, sl = kernels.sss(d(pairs), d(g["crystal"]), d(g["scatter"]), d(g["sumup"]), d(g["atten"]),
+                         d(g["umap"]), list(g["usize"]), int(g["ncpr"]), int(g["nbpr"]),
+                         list(g["grid_block"]), int(g["low"]), int(g["high"]), float(g["res"]))
+    sc, sl = sc.cpu().numpy(), sl.cpu().numpy()
+    assert rel_l2(sc, ref_s) <= 1e-5
+    np.testing.assert_allclose(sc, ref_s, rtol=2e-5, atol=1e-6 * np.abs(ref_s).max())
+    ok = np.isfinite(ref_c) & (ref_c < 1e6)
+    np.testing.assert_allclose(sl[ok], ref_c[ok], rtol=1e-5)
+
+
+def test_scatter_correct_pipeline_matches_oracle(cuda_lib, oracle, small_case):
+    import srf_gb300 as nef
+    from srf_gb300 import scatter as S
+    sc = small_case["scanner"]
+    rng = np.random.default_rng(4)
+    shape, size = [32, 32, 16], [128.0, 128.0, 128.0]
+    emission = nef.Image(rng.random(shape).astype(np.float32), [0.0, 0.0, 0.0], size)
+    umap = nef.Umap((rng.random(shape) * 0.01).astype(np.float32), [0.0, 0.0, 0.0], size)
+    lors = small_case["lors"][:4000, :6]
+    lm = nef.Listmode(np.ones(len(lors), np.float32), nef.Lors(lors))
+    corr = S.ScatterCorrect(350, 650, 0.15, 0.3)
+    pre = S.scatter_preprocess(sc, lm, emission, umap)
+    ref_pre = oracle.scatter_preprocess(sc, lm, emission, umap)
+    for k in ("sumup_emission", "atten", "atten_lors"):
+        assert rel_l2(pre[k], ref_pre[k]) <= 1e-5, k
+    for k in ("lors", "sinogram", "index", "scatter_position", "crystal_position"):
+        assert np.array_equal(pre[k], ref_pre[k]), k
+    out = corr(emission, umap, sc, pre)
+    ref = oracle.scatter_correct(corr, emission, umap, sc, ref_pre)
+    assert out.lors.data.shape == ref.lors.data.shape
+    assert np.array_equal(out.lors.data[:, :6], ref.lors.data[:, :6])
+    assert rel_l2(out.data, ref.data) <= 1e-5

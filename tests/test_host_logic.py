@@ -1,0 +1,107 @@
+"""Host-side logic without a GPU: geometry index arithmetic, data containers, sinogram formats and
+scatter-point placement against the reference's own host code (golden host.npz)."""
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def host():
+    return dict(np.load(os.path.join(HERE, "golden", "host.npz")))
+
+
+def test_get_all_lors_id(host):
+    from srf_gb300.scatter import get_all_lors_id
+    got = get_all_lors_id(int(host["n"]))
+    assert got.dtype == np.int32
+    assert np.array_equal(got, host["all_ids"])
+
+
+def test_lm2sino_matches_cal_sinogram(host):
+    from srf_gb300 import synth
+    from srf_gb300.data import Listmode, Lors
+    from srf_gb300.geometry import EcatIndexToCrystalPos, PetEcatScanner, Block, TofConfig
+    from srf_gb300.scatter import lm2sino
+    # a scanner with exactly n = 37 crystals is not an ECAT geometry; map the golden ids onto
+    # a 40-crystal scanner and compare bins of the first 37 crystals
+    sc = PetEcatScanner(99.0, 119.0, 1, 10, 0.0, Block([20.0, 16.0, 3.2], [1, 4, 1]), TofConfig())
+    pos = EcatIndexToCrystalPos(sc)(np.arange(sc.nb_crystals))
+    id1, id2, w = host["id1"], host["id2"], host["w"]
+    lors = np.hstack([pos[id1], pos[id2]]).astype(np.float32)
+    sino = lm2sino(Listmode(w, Lors(lors)), sc)
+    n = int(host["n"])
+    ref = host["sino"][:, 0]
+    assert np.allclose(sino[: ref.size, 0], ref, rtol=0, atol=1e-12)
+
+
+def test_scatter_positions(host):
+    from srf_gb300.data import Image
+    from srf_gb300.scatter import pre_all_scatter_position
+    img = Image(np.zeros(tuple(host["img_shape"]), np.float32), [0.0, 0.0, 0.0], list(host["img_size"]))
+    got = pre_all_scatter_position(img)
+    assert got.dtype == np.float32
+    assert np.array_equal(got, host["scatter_position"])
+
+
+def test_crystal_index_round_trip():
+    from srf_gb300 import synth
+    from srf_gb300.geometry import EcatCrystalPosToIndex, EcatIndexToCrystalPos, block_full_crystal_table
+    for sc in (synth.scanner_small(), synth.scanner_clinical()):
+        ids = np.arange(sc.nb_crystals)
+        pos = EcatIndexToCrystalPos(sc)(ids)
+        assert pos.dtype == np.float32 and pos.shape == (sc.nb_crystals, 3)
+        assert np.array_equal(EcatCrystalPosToIndex(sc)(pos), ids)
+        r = np.hypot(pos[:, 0], pos[:, 1])
+        assert r.min() >= sc.average_radius - 1e-3
+        # 'block-full' table: row i*M + m is crystal m of block column i (m over all rings)
+        table = block_full_crystal_table(sc)
+        pb, M = sc.nb_crystals_per_block, sc.nb_crystals_per_block * sc.nb_rings
+        i, m = np.divmod(np.arange(table.shape[0]), M)
+        full = (m % pb) + i * pb + (m // pb) * sc.nb_crystals_per_ring
+        assert np.abs(table - pos[full]).max() < 1e-3
+
+
+def test_listmode_trans_snaps_and_keeps_tof():
+    from srf_gb300 import synth
+    from srf_gb300.data import Listmode, Lors
+    from srf_gb300.geometry import EcatIndexToCrystalPos, PetEcatListmodeTrans
+    sc = synth.scanner_small()
+    pos = EcatIndexToCrystalPos(sc)(np.arange(sc.nb_crystals))
+    rng = np.random.default_rng(0)
+    a, b = rng.integers(0, sc.nb_crystals, 50), rng.integers(0, sc.nb_crystals, 50)
+    jitter = rng.uniform(-0.4, 0.4, (50, 6)).astype(np.float32)
+    tof = rng.normal(0, 30, (50, 1)).astype(np.float32)
+    lors = np.hstack([np.hstack([pos[a], pos[b]]) + jitter, tof]).astype(np.float32)
+    out = PetEcatListmodeTrans(sc)(Listmode(np.ones(50, np.float32), Lors(lors)))
+    assert np.array_equal(out.lors.data[:, :3], pos[a]) and np.array_equal(out.lors.data[:, 3:6], pos[b])
+    assert np.array_equal(out.lors.data[:, 6], tof[:, 0])
+
+
+def test_containers_are_frozen_records():
+    import dataclasses
+    from srf_gb300.data import Image, Listmode, Lors
+    img = Image(np.ones((4, 5, 6), np.float32), [0, 0, 0], [8.0, 10.0, 12.0])
+    assert img.shape == [4, 5, 6] and img.unit_size == [2.0, 2.0, 2.0]
+    with pytest.raises(dataclasses.FrozenInstanceError):
+        img.data = None
+    img2 = (img * 2).update(center=[1, 1, 1])
+    assert img2.center == [1, 1, 1] and float(img2.data.sum()) == 240.0 and img.center == [0, 0, 0]
+    lm = Listmode(np.ones(3, np.float32), Lors(np.zeros((3, 7), np.float32)))
+    assert len(lm) == 3 and lm.lors.tof_values.shape == (3,)
+    assert len(lm.append(lm)) == 6
+
+
+def test_synthetic_events_are_snapped_and_seeded():
+    from srf_gb300 import synth
+    from srf_gb300.geometry import EcatCrystalPosToIndex, EcatIndexToCrystalPos
+    sc, ic = synth.scanner_small(), synth.image_small()
+    act = synth.phantom_cylinder(ic)
+    a = synth.sample_events(sc, ic, act, 500, seed=3, tof_fwhm_ps=530.0).numpy()
+    b = synth.sample_events(sc, ic, act, 500, seed=3, tof_fwhm_ps=530.0).numpy()
+    assert np.array_equal(a, b) and a.shape == (500, 7)
+    ids = EcatCrystalPosToIndex(sc)(a[:, :3])
+    assert np.array_equal(EcatIndexToCrystalPos(sc)(ids), a[:, :3])
+    assert abs(float(np.std(a[:, 6])) - 70) < 25  # TOF spread: sigma(d2-d1) = 67.5 mm plus geometry
