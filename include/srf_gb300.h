@@ -90,6 +90,22 @@ int srf_backprojection_tof(const float *lors, int64_t n, int32_t lor_stride,
                            const int32_t grid[3], const float center[3], const float size[3],
                            void *stream);
 
+/* srf_backprojection_tof without any device allocation. No counterpart in the reference.
+ * For callers that cannot call cudaMalloc (a plugin inside a framework that owns the device memory,
+ * or an acquisition service with a fixed device-memory reservation): the y-dominant LORs are
+ * accumulated in a static device array of SRF_NOALLOC_MAX_VOXELS floats (18 MiB, held by every GPU
+ * that loads the library) and folded into `image` (x-fastest, strides {1, nx, nx*ny}), which is
+ * accumulated into like srf_backprojection_tof. Grids with more voxels return SRF_ERANGE. The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture. All calls share the array: calls that overlap on the GPU race. */
+#define SRF_NOALLOC_MAX_VOXELS 4718592
+int srf_backprojection_tof_noalloc(const float *lors, int64_t n, int32_t lor_stride,
+                                   const float *tof, int32_t tof_stride,
+                                   float tof_bin, float tof_sigma2, float tof_nsigma,
+                                   const float *values, float *image,
+                                   const int32_t grid[3], const float center[3], const float size[3],
+                                   void *stream);
+
 /* image += P^T values for the projector P of srf_projection (tof == NULL) or
  * srf_projection_tof: the exact adjoint (projector rules, 1/L^2 weights), used as the backward
  * of the differentiable projector. The reference's backprojector is not this adjoint. */
