@@ -48,6 +48,10 @@ int srf_version(void);
 /* Lanes per LOR used by the traversal kernels (8, 16 or 32; default 32). Process-wide. */
 int srf_set_group_lanes(int lanes);
 
+/* Lanes per LOR and slabs per lane per chunk of the fused OSEM kernel (2 or 4; default 4).
+ * Process-wide; chosen by srf_gb300.autotune. */
+int srf_set_tuning(int lanes, int slabs_per_lane);
+
 /* ------------------------------------------------------------------ projector family */
 
 /* p[i] = sum_v A_iv image_v, non-TOF.

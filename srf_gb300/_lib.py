@@ -23,7 +23,7 @@ SRF_RATIO_PLAIN = 1
 
 # every symbol include/srf_gb300.h declares
 EXPORTS = (
-    "srf_last_error", "srf_version", "srf_set_group_lanes", "srf_projection", "srf_backprojection",
+    "srf_last_error", "srf_version", "srf_set_group_lanes", "srf_set_tuning", "srf_projection", "srf_backprojection",
     "srf_projection_tof", "srf_backprojection_tof", "srf_projection_adjoint", "srf_fold_views",
     "srf_copy_view", "srf_count_pairs", "srf_osem_subset", "srf_osem_update", "srf_emap_block_full", "srf_sss",
     "srf_backprojection_tof_noalloc",
@@ -123,3 +123,7 @@ def yfast_strides(shape):
 
 def set_group_lanes(lanes: int) -> None:
     call("srf_set_group_lanes", ctypes.c_int(lanes))
+
+
+def set_tuning(lanes: int, slabs_per_lane: int) -> None:
+    call("srf_set_tuning", ctypes.c_int(lanes), ctypes.c_int(slabs_per_lane))

@@ -7,7 +7,7 @@
 #include <cmath>
 #include <cuda_runtime.h>
 
-#include "../../include/srf_gb300.h"
+#include "srf_gb300.h"
 #include "siddon.cuh"
 
 namespace srf {
@@ -49,6 +49,12 @@ inline int num_sms() {
 inline int &group_lanes() {
     static int lanes = 32;
     return lanes;
+}
+
+// Slabs each lane of a LOR group handles per chunk in the fused OSEM kernel (2 or 4; default 4).
+inline int &slabs_per_lane() {
+    static int u = 4;
+    return u;
 }
 
 constexpr int kBlock = 256;

@@ -18,12 +18,33 @@
 
 namespace srf {
 
-// per-LOR record in shared memory
-struct LorRec {
-    float p1, p2, q1, z1, kq, kz, wc, invL2, ratio1, L, yv;
-    int lo, hi, flags;
+// Per-LOR record in shared memory: everything the slab loop needs, computed once per LOR by one
+// lane (setup_rec) and read by the LOR's group as six 16-byte broadcasts.
+struct __align__(16) LorRec {
+    float p1, p2, q1, z1;
+    float kq, kz, wc, invL2;
+    float ratio1, L, yv, pd;
+    float inv_pd, Aq, Bq, Az;  // fast forms: boundary(pp) ~= fmaf(B, pp, A)
+    float Bz, mq, mz, pad0;    // mq, mz: floor margins of the fast forms
+    int lo, hi, flags, pad1;
 };
 constexpr int F_VALID = 1, F_PROJ = 2, F_XDOM = 4, F_TIE = 8;
+
+__device__ __forceinline__ LorRec load_rec(const LorRec *src) {
+    LorRec R;
+    const float4 *s4 = reinterpret_cast<const float4 *>(src);
+    float4 *d4 = reinterpret_cast<float4 *>(&R);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) d4[c] = s4[c];
+    return R;
+}
+
+__device__ __forceinline__ void store_rec(LorRec *dst, const LorRec &R) {
+    const float4 *s4 = reinterpret_cast<const float4 *>(&R);
+    float4 *d4 = reinterpret_cast<float4 *>(dst);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) d4[c] = s4[c];
+}
 
 // grid-wide constants, rounded exactly as in setup_lor
 struct GridK {
@@ -60,7 +81,7 @@ __device__ __forceinline__ GridK make_gridk(const Grid &g, const TofParams &tp) 
 template <bool TOF>
 __device__ __forceinline__ LorRec setup_rec(const float *l, float tv, float yv, const Grid &g,
                                             const GridK &k) {
-    LorRec R;
+    LorRec R = {};
     R.flags = 0;
     R.lo = 1;
     R.hi = 0;
@@ -118,16 +139,29 @@ __device__ __forceinline__ LorRec setup_rec(const float *l, float tv, float yv, 
     R.lo = max(lo, 0);
     R.hi = min(hi, np - 1);
     if (R.lo > R.hi && !(R.flags & F_TIE)) R.flags = 0;
+    // fast forms of the boundary coordinates and their floor margins: both the fast form and the
+    // reference's operand sequence are within a few units of 2^-24 * S of the exact value,
+    // S = (|k| (|p1| + np) + |a|) / d + |n2| + 2 over the LOR's slabs; 2^-20 * S bounds their
+    // difference with room to spare.
+    R.pd = pd;
+    R.inv_pd = 1.0f / pd;
+    R.Bq = R.kq / dq;
+    R.Aq = (R.q1 - R.kq * R.p1) / dq + nq2;
+    R.Bz = R.kz / k.dz;
+    R.Az = (z1 - R.kz * R.p1) / k.dz + k.nz2;
+    const float e = 9.5367431640625e-7f;  // 2^-20
+    R.mq = e * ((fabsf(R.kq) * (fabsf(R.p1) + (float)np) + fabsf(R.q1)) / dq + nq2 + 2.0f);
+    R.mz = e * ((fabsf(R.kz) * (fabsf(R.p1) + (float)np) + fabsf(z1)) / k.dz + k.nz2 + 2.0f);
+    R.pad0 = 0.0f;
+    R.pad1 = 0;
     return R;
 }
 
-// Per-LOR constants of the slab loop, derived from a record.
+// Per-LOR constants of the slab loop: the record plus the axis-dependent grid values.
 struct LorRun {
     float p1, p2, q1, z1, kq, kz, wc, pd, ratio1, L;
     float np2, nq2, dq, dpc;
-    // fast forms: boundary(pp) ~= fmaf(B, pp, A); TOF d2 ~= ((pc - p1) * inv_pd - ratio1) * L
-    float Aq, Bq, Az, Bz, inv_pd;
-    float mq, mz;  // floor margins of the fast forms (bounds on |fast - reference rounding|)
+    float Aq, Bq, Az, Bz, inv_pd, mq, mz;
     int np, nq, nz, np_half, lo, hi;
     int32_t sp, sq, szs;
     bool xdom, dq_one;
@@ -139,9 +173,10 @@ __device__ __forceinline__ LorRun make_run(const LorRec &R, const Grid &g, const
     LorRun r;
     r.xdom = R.flags & F_XDOM;
     r.p1 = R.p1; r.p2 = R.p2; r.q1 = R.q1; r.z1 = R.z1; r.kq = R.kq; r.kz = R.kz; r.wc = R.wc;
-    r.pd = __fsub_rn(R.p2, R.p1);
+    r.pd = R.pd;
     r.ratio1 = R.ratio1;
     r.L = R.L;
+    r.Aq = R.Aq; r.Bq = R.Bq; r.Az = R.Az; r.Bz = R.Bz; r.inv_pd = R.inv_pd; r.mq = R.mq; r.mz = R.mz;
     r.np = r.xdom ? g.nx : g.ny;
     r.nq = r.xdom ? g.ny : g.nx;
     r.nz = g.nz;
@@ -153,17 +188,6 @@ __device__ __forceinline__ LorRun make_run(const LorRec &R, const Grid &g, const
     r.np_half = r.np / 2;
     r.lo = R.lo;
     r.hi = R.hi;
-    r.Bq = r.kq / r.dq;
-    r.Aq = (r.q1 - r.kq * r.p1) / r.dq + r.nq2;
-    r.Bz = r.kz / k.dz;
-    r.Az = (r.z1 - r.kz * r.p1) / k.dz + k.nz2;
-    r.inv_pd = 1.0f / r.pd;
-    // Both the fast form and the reference's operand sequence are within a few units of
-    // 2^-24 * S of the exact value, S = (|k| (|p1| + |pp|) + |a|) / d + |n2| + 2 with |pp| <= np;
-    // 2^-20 * S (16 units) bounds their difference with room to spare.
-    const float e = 9.5367431640625e-7f;  // 2^-20
-    r.mq = e * ((fabsf(r.kq) * (fabsf(r.p1) + (float)r.np) + fabsf(r.q1)) / r.dq + r.nq2 + 2.0f);
-    r.mz = e * ((fabsf(r.kz) * (fabsf(r.p1) + (float)r.np) + fabsf(r.z1)) / k.dz + k.nz2 + 2.0f);
     const int64_t *st = (!r.xdom && have_t) ? sty : stx;
     r.sp = (int32_t)(r.xdom ? st[0] : st[1]);
     r.sq = (int32_t)(r.xdom ? st[1] : st[0]);
@@ -178,89 +202,107 @@ __device__ __forceinline__ bool near_int(float t, float m) {
     return f < m || f > 1.0f - m;
 }
 
-// Relative margin on the TOF truncation test t2 <= nsigma^2 (fast t2 is within ~1e-6 relative).
+// Relative margin on the TOF truncation test t2 <= nsigma^2 (fast t2 is within ~1e-5 relative).
 constexpr float kTruncMargin = 2e-4f;
 
-// Voxel candidates of slab ip (branch-free form of the reference's case analysis,
-// siddon.cu.cc:86-189). w[k] == 0 marks a voxel that is not visited. Also returns the
-// projector's slab predicate in pm.
+// Voxels of one slab from the (already floored) boundary coordinates: the branch-free form of the
+// reference's case analysis (siddon.cu.cc:86-189). w[c] == 0 marks a voxel that is not visited.
+__device__ __forceinline__ void slab_voxels(const LorRun &r, int ip, bool keep, float qq1, float qq2,
+                                            float zz1, float zz2, float wt, int32_t o[3], float w[3]) {
+    const int cq1 = ifloor(qq1), cq2 = ifloor(qq2);
+    const int cz1 = ifloor(zz1), cz2 = ifloor(zz2);
+    const bool dq = cq1 != cq2, dz = cz1 != cz2;
+    const bool R = keep && (dq ? (cq1 >= -1) : (cq1 >= 0)) && cq1 < r.nq &&
+                   (dz ? (cz1 >= -1) : (cz1 >= 0)) && cz1 < r.nz;
+    const float rq = dq ? __fdividef((float)cq2 - qq1, qq2 - qq1) : 0.0f;
+    const float rz = dz ? __fdividef((float)cz2 - zz1, zz2 - zz1) : 0.0f;
+    const int32_t base = ip * r.sp;
+    // near corner (cq1, cz1)
+    const bool v0 = R && cq1 >= 0 && cz1 >= 0;
+    const float f0 = dq ? (dz ? fminf(rq, rz) : rq) : (dz ? rz : 1.0f);
+    o[0] = v0 ? base + cq1 * r.sq + cz1 * r.szs : 0;
+    w[0] = v0 ? f0 * wt : 0.0f;
+    // far corner (cq2, cz2)
+    const bool v2 = R && (dq || dz) && cq2 < r.nq && cz2 < r.nz;
+    const float f2 = 1.0f - (dq ? (dz ? fmaxf(rq, rz) : rq) : rz);
+    o[2] = v2 ? base + cq2 * r.sq + cz2 * r.szs : 0;
+    w[2] = v2 ? f2 * wt : 0.0f;
+    // middle voxel when both coordinates step: z first -> (cq1, cz2), else (cq2, cz1)
+    const bool qfirst = rq > rz;
+    const int mq = qfirst ? cq1 : cq2, mz = qfirst ? cz2 : cz1;
+    const bool v1 = R && dq && dz && mq >= 0 && mq < r.nq && mz >= 0 && mz < r.nz;
+    o[1] = v1 ? base + mq * r.sq + mz * r.szs : 0;
+    w[1] = v1 ? (qfirst ? (rq - rz) : (rz - rq)) * wt : 0.0f;
+}
+
+__device__ __forceinline__ bool proj_slab_rule(const LorRun &r, bool tof, float pp1, float pp2) {
+    if (!tof) return !((r.p1 < r.p2 && pp2 > r.p2) || (r.p1 >= r.p2 && pp1 < r.p2));
+    if (r.xdom) return !((r.p2 > r.p1 && pp1 <= r.p1) || (r.p2 < r.p1 && pp2 >= r.p1));
+    return !((r.p2 > r.p1 && pp1 < r.p1) || (r.p2 < r.p1 && pp2 > r.p1));
+}
+
+// Fast, branch-free candidates of slab ip. `bad` is set when a floor or the truncation test is
+// within its rounding margin; the caller then recomputes the slab with candidates_exact.
 template <bool TOF>
-__device__ __forceinline__ void candidates(const LorRun &r, const GridK &k, int ip, int32_t o[3],
-                                           float w[3], bool &pm) {
-    w[0] = w[1] = w[2] = 0.0f;
-    o[0] = o[1] = o[2] = 0;
-    pm = false;
+__device__ __forceinline__ void candidates_fast(const LorRun &r, const GridK &k, int ip, bool active,
+                                                int32_t o[3], float w[3], bool &pm, bool &bad) {
+    bool keep = active;
+    bad = false;
     float w_tof = 1.0f;
     if (TOF) {
         const float pc = __fmul_rn(__fadd_rn((float)(ip - r.np_half), 0.5f), r.dpc);
         const float d2 = ((pc - r.p1) * r.inv_pd - r.ratio1) * r.L;
-        float t2 = d2 * d2 * k.inv_expand;
+        const float t2 = d2 * d2 * k.inv_expand;
         if (k.nsig2 > 0.0f) {
-            if (fabsf(t2 - k.nsig2) <= kTruncMargin * k.nsig2) {
-                const float d2e = __fmul_rn(__fsub_rn(__fdiv_rn(__fsub_rn(pc, r.p1), r.pd), r.ratio1), r.L);
-                t2 = __fdiv_rn(__fmul_rn(d2e, d2e), k.expand);
-            }
-            if (t2 > k.nsig2) return;
+            bad = fabsf(t2 - k.nsig2) <= kTruncMargin * k.nsig2;
+            keep = keep && (t2 <= k.nsig2);
         }
         w_tof = k.tof_amp * exp2f(t2 * -0.72134752044448170f);  // exp(-t2/2)
     }
     const float pp1 = __fsub_rn((float)ip, r.np2);
     const float pp2 = __fadd_rn(pp1, 1.0f);
-    if (!TOF) {
-        pm = !((r.p1 < r.p2 && pp2 > r.p2) || (r.p1 >= r.p2 && pp1 < r.p2));
-    } else if (r.xdom) {
-        pm = !((r.p2 > r.p1 && pp1 <= r.p1) || (r.p2 < r.p1 && pp2 >= r.p1));
-    } else {
-        pm = !((r.p2 > r.p1 && pp1 < r.p1) || (r.p2 < r.p1 && pp2 > r.p1));
-    }
+    pm = proj_slab_rule(r, TOF, pp1, pp2);
     float qa, qb;
     if (r.dq_one) {  // exact and cheap without a division
-        qa = bcoord(r.q1, r.kq, pp1, r.p1, 1.0f, r.nq2, true);
-        qb = bcoord(r.q1, r.kq, pp2, r.p1, 1.0f, r.nq2, true);
+        qa = __fadd_rn(__fadd_rn(r.q1, __fmul_rn(r.kq, __fsub_rn(pp1, r.p1))), r.nq2);
+        qb = __fadd_rn(__fadd_rn(r.q1, __fmul_rn(r.kq, __fsub_rn(pp2, r.p1))), r.nq2);
     } else {
         qa = fmaf(r.Bq, pp1, r.Aq);
         qb = fmaf(r.Bq, pp2, r.Aq);
-        if (near_int(qa, r.mq)) qa = bcoord(r.q1, r.kq, pp1, r.p1, r.dq, r.nq2, false);
-        if (near_int(qb, r.mq)) qb = bcoord(r.q1, r.kq, pp2, r.p1, r.dq, r.nq2, false);
+        bad = bad || near_int(qa, r.mq) || near_int(qb, r.mq);
     }
-    float za = fmaf(r.Bz, pp1, r.Az);
-    float zb = fmaf(r.Bz, pp2, r.Az);
-    if (near_int(za, r.mz)) za = bcoord(r.z1, r.kz, pp1, r.p1, k.dz, k.nz2, false);
-    if (near_int(zb, r.mz)) zb = bcoord(r.z1, r.kz, pp2, r.p1, k.dz, k.nz2, false);
+    const float za = fmaf(r.Bz, pp1, r.Az);
+    const float zb = fmaf(r.Bz, pp2, r.Az);
+    bad = active && (bad || near_int(za, r.mz) || near_int(zb, r.mz));
     const float qq1 = (r.kq >= 0.0f) ? qa : qb, qq2 = (r.kq >= 0.0f) ? qb : qa;
     const float zz1 = (r.kz >= 0.0f) ? za : zb, zz2 = (r.kz >= 0.0f) ? zb : za;
-    const int cq1 = ifloor(qq1), cq2 = ifloor(qq2);
-    const int cz1 = ifloor(zz1), cz2 = ifloor(zz2);
-    const bool dq = cq1 != cq2, dz = cz1 != cz2;
-    // the case's range condition
-    const bool R = (dq ? (cq1 >= -1) : (cq1 >= 0)) && cq1 < r.nq &&
-                   (dz ? (cz1 >= -1) : (cz1 >= 0)) && cz1 < r.nz;
-    if (!R) return;
-    const float rq = dq ? __fdividef((float)cq2 - qq1, qq2 - qq1) : 0.0f;
-    const float rz = dz ? __fdividef((float)cz2 - zz1, zz2 - zz1) : 0.0f;
-    const float wt = r.wc * w_tof;
-    const int32_t base = ip * r.sp;
-    // near corner (cq1, cz1)
-    const float f0 = dq ? (dz ? fminf(rq, rz) : rq) : (dz ? rz : 1.0f);
-    if (cq1 >= 0 && cz1 >= 0) {
-        o[0] = base + cq1 * r.sq + cz1 * r.szs;
-        w[0] = f0 * wt;
+    slab_voxels(r, ip, keep, qq1, qq2, zz1, zz2, r.wc * w_tof, o, w);
+}
+
+// The same slab with the reference's operand sequence for every value that decides a floor or
+// the truncation test (IEEE division, no contraction).
+template <bool TOF>
+__device__ __forceinline__ void candidates_exact(const LorRun &r, const GridK &k, int ip, int32_t o[3],
+                                              float w[3], bool &pm) {
+    bool keep = true;
+    float w_tof = 1.0f;
+    if (TOF) {
+        const float pc = __fmul_rn(__fadd_rn((float)(ip - r.np_half), 0.5f), r.dpc);
+        const float d2 = __fmul_rn(__fsub_rn(__fdiv_rn(__fsub_rn(pc, r.p1), r.pd), r.ratio1), r.L);
+        const float t2 = __fdiv_rn(__fmul_rn(d2, d2), k.expand);
+        if (k.nsig2 > 0.0f) keep = t2 <= k.nsig2;
+        w_tof = k.tof_amp * exp2f(t2 * -0.72134752044448170f);
     }
-    // far corner (cq2, cz2)
-    if ((dq || dz) && cq2 < r.nq && cz2 < r.nz) {
-        const float f2 = 1.0f - (dq ? (dz ? fmaxf(rq, rz) : rq) : rz);
-        o[2] = base + cq2 * r.sq + cz2 * r.szs;
-        w[2] = f2 * wt;
-    }
-    // middle voxel when both coordinates step
-    if (dq && dz) {
-        const bool qfirst = rq > rz;  // z steps first: (cq1, cz2); else (cq2, cz1)
-        const int mq = qfirst ? cq1 : cq2, mz = qfirst ? cz2 : cz1;
-        if (mq >= 0 && mq < r.nq && mz >= 0 && mz < r.nz) {
-            o[1] = base + mq * r.sq + mz * r.szs;
-            w[1] = (qfirst ? (rq - rz) : (rz - rq)) * wt;
-        }
-    }
+    const float pp1 = __fsub_rn((float)ip, r.np2);
+    const float pp2 = __fadd_rn(pp1, 1.0f);
+    pm = proj_slab_rule(r, TOF, pp1, pp2);
+    const float qa = bcoord(r.q1, r.kq, pp1, r.p1, r.dq, r.nq2, r.dq_one);
+    const float qb = bcoord(r.q1, r.kq, pp2, r.p1, r.dq, r.nq2, r.dq_one);
+    const float za = bcoord(r.z1, r.kz, pp1, r.p1, k.dz, k.nz2, false);
+    const float zb = bcoord(r.z1, r.kz, pp2, r.p1, k.dz, k.nz2, false);
+    const float qq1 = (r.kq >= 0.0f) ? qa : qb, qq2 = (r.kq >= 0.0f) ? qb : qa;
+    const float zz1 = (r.kz >= 0.0f) ? za : zb, zz2 = (r.kz >= 0.0f) ? zb : za;
+    slab_voxels(r, ip, keep, qq1, qq2, zz1, zz2, r.wc * w_tof, o, w);
 }
 
 }  // namespace srf

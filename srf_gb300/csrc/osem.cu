@@ -12,8 +12,6 @@
 
 namespace srf {
 
-constexpr int kUnroll = 4;  // slabs per lane per chunk
-
 // Generic path for a LOR whose projector and backprojector traverse along different axes
 // (non-TOF with |xd| == |yd|): two setups, as in the standalone kernels.
 template <int G, bool TOF>
@@ -39,11 +37,29 @@ __device__ __forceinline__ void tie_path(const float *l, float tv, float yv, int
     }
 }
 
+// U slabs of one chunk per lane: fast candidates for all (independent, so they interleave), then
+// the rare exact recomputation of the slabs whose floors sat within the rounding margin.
+template <bool TOF, int U>
+__device__ __forceinline__ void chunk_candidates(const LorRun &run, const GridK &k, int c0, int lane,
+                                                 int G, int32_t (&o)[U][3], float (&w)[U][3],
+                                                 bool (&pm)[U]) {
+    bool bad[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int ip = c0 + lane + G * u;
+        const bool act = ip <= run.hi;
+        candidates_fast<TOF>(run, k, act ? ip : run.hi, act, o[u], w[u], pm[u], bad[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+        if (bad[u]) candidates_exact<TOF>(run, k, c0 + lane + G * u, o[u], w[u], pm[u]);
+}
+
 // One warp handles 32 consecutive LORs per round: lane j sets up LOR j into shared memory, then
-// the warp's 32/G groups walk the records. x/x_t and bp/bp_t must have equal strides (offsets are
+// the warp's 32/G groups walk the records. x/x_t and bp/bp_t have equal strides (offsets are
 // computed once for the gather and the scatter).
-template <int G, bool TOF>
-__global__ void __launch_bounds__(kBlock, 2)
+template <int G, bool TOF, int U, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB)
 k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
               int tof_stride, Grid g, TofParams tp, const float *__restrict__ y, int rule, float eps,
               View x, View xt, View bp, View bpt, double *__restrict__ loglik) {
@@ -60,10 +76,10 @@ k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float
     const bool want_ll = loglik != nullptr;
     double ll = 0.0;
     for (int64_t base = warp * 32; base < n; base += nwarps * 32) {
-        // lane-parallel setup of the warp's next 32 LORs
-        {
+        {  // lane-parallel setup of the warp's next 32 LORs
             const int64_t i = base + lane32;
-            LorRec R;
+            LorRec R = {};
+            R.lo = 1;
             if (i < n) {
                 const float *l = lors + i * stride;
                 float lv[6];
@@ -72,20 +88,15 @@ k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float
                 const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
                 const float yv = y ? __ldg(y + i) : 1.0f;
                 R = setup_rec<TOF>(lv, tv, yv, g, k);
-            } else {
-                R.flags = 0;
-                R.lo = 1;
-                R.hi = 0;
             }
-            recs[wib][lane32] = R;
+            store_rec(&recs[wib][lane32], R);
         }
         __syncwarp();
         for (int j0 = 0; j0 < 32; j0 += GPW) {
             const int j = j0 + gi;
-            const LorRec R = recs[wib][j];
+            const LorRec R = load_rec(&recs[wib][j]);
             const int64_t i = base + j;
             if (R.flags & F_TIE) {
-                // rare: re-read the LOR and take the two-setup path
                 float lv[6];
                 const float *l = lors + i * stride;
 #pragma unroll
@@ -99,33 +110,23 @@ k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float
             const float *xim = (!run.xdom && have_t) ? xt.ptr : x.ptr;
             float *bim = (!run.xdom && have_t) ? bpt.ptr : bp.ptr;
             const bool proj_ok = R.flags & F_PROJ;
-            const bool single = (run.hi - run.lo + 1) <= G * kUnroll;
-            int32_t o[kUnroll][3];
-            float w[kUnroll][3];
+            const bool single = (run.hi - run.lo + 1) <= G * U;
+            int32_t o[U][3];
+            float w[U][3];
+            bool pm[U];
             float acc = 0.0f;
             if (valid) {
-                for (int c0 = run.lo; c0 <= run.hi; c0 += G * kUnroll) {
-                    bool pm[kUnroll];
-#pragma unroll
-                    for (int u = 0; u < kUnroll; ++u) {
-                        const int ip = c0 + lane + G * u;
-                        if (ip <= run.hi) {
-                            candidates<TOF>(run, k, ip, o[u], w[u], pm[u]);
-                        } else {
-                            o[u][0] = o[u][1] = o[u][2] = 0;
-                            w[u][0] = w[u][1] = w[u][2] = 0.0f;
-                            pm[u] = false;
-                        }
-                    }
+                for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
+                    chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
                     if (proj_ok) {
-                        float xv[kUnroll][3];
+                        float xv[U][3];
 #pragma unroll
-                        for (int u = 0; u < kUnroll; ++u)
+                        for (int u = 0; u < U; ++u)
 #pragma unroll
                             for (int c = 0; c < 3; ++c)
                                 xv[u][c] = (pm[u] && w[u][c] != 0.0f) ? __ldg(xim + o[u][c]) : 0.0f;
 #pragma unroll
-                        for (int u = 0; u < kUnroll; ++u)
+                        for (int u = 0; u < U; ++u)
 #pragma unroll
                             for (int c = 0; c < 3; ++c) acc = fmaf(xv[u][c], w[u][c], acc);
                     }
@@ -143,24 +144,18 @@ k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float
             if (r == 0.0f) continue;
             if (single) {
 #pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
+                for (int u = 0; u < U; ++u)
 #pragma unroll
                     for (int c = 0; c < 3; ++c)
                         if (w[u][c] != 0.0f) atomicAdd(bim + o[u][c], r * w[u][c]);
             } else {
-                for (int c0 = run.lo; c0 <= run.hi; c0 += G * kUnroll) {
+                for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
+                    chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
 #pragma unroll
-                    for (int u = 0; u < kUnroll; ++u) {
-                        const int ip = c0 + lane + G * u;
-                        if (ip > run.hi) break;
-                        int32_t oo[3];
-                        float ww[3];
-                        bool pmu;
-                        candidates<TOF>(run, k, ip, oo, ww, pmu);
+                    for (int u = 0; u < U; ++u)
 #pragma unroll
                         for (int c = 0; c < 3; ++c)
-                            if (ww[c] != 0.0f) atomicAdd(bim + oo[c], r * ww[c]);
-                    }
+                            if (w[u][c] != 0.0f) atomicAdd(bim + o[u][c], r * w[u][c]);
                 }
             }
         }
@@ -173,15 +168,25 @@ k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float
     }
 }
 
-template <int G, bool TOF>
+template <int G, bool TOF, int U, int MINB>
 static int launch_osem_g(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
                          const Grid &g, const TofParams &tp, const float *y, int rule, float eps,
                          const View &x, const View &xt, const View &bp, const View &bpt,
                          double *loglik, cudaStream_t s) {
-    auto kern = k_osem_subset<G, TOF>;
+    auto kern = k_osem_subset<G, TOF, U, MINB>;
     unsigned blocks = grid_for(kern, n, kBlock);
     kern<<<blocks, kBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik);
     return check_cuda("osem subset kernel launch");
+}
+
+template <int G, bool TOF>
+static int launch_osem_u(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                         const Grid &g, const TofParams &tp, const float *y, int rule, float eps,
+                         const View &x, const View &xt, const View &bp, const View &bpt,
+                         double *loglik, cudaStream_t s) {
+    if (slabs_per_lane() == 2)
+        return launch_osem_g<G, TOF, 2, 3>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
+    return launch_osem_g<G, TOF, 4, 2>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
 }
 
 template <bool TOF>
@@ -190,9 +195,9 @@ static int launch_osem(const float *lors, int64_t n, int stride, const float *to
                        const View &x, const View &xt, const View &bp, const View &bpt,
                        double *loglik, cudaStream_t s) {
     switch (group_lanes()) {
-    case 8: return launch_osem_g<8, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
-    case 16: return launch_osem_g<16, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
-    default: return launch_osem_g<32, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
+    case 8: return launch_osem_u<8, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
+    case 16: return launch_osem_u<16, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
+    default: return launch_osem_u<32, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
     }
 }
 

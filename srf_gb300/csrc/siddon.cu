@@ -114,6 +114,14 @@ int srf_set_group_lanes(int lanes) {
     return ok();
 }
 
+int srf_set_tuning(int lanes, int slabs_per_lane_) {
+    if (lanes != 8 && lanes != 16 && lanes != 32) return fail(SRF_EINVAL, "lanes must be 8, 16 or 32");
+    if (slabs_per_lane_ != 2 && slabs_per_lane_ != 4) return fail(SRF_EINVAL, "slabs_per_lane must be 2 or 4");
+    group_lanes() = lanes;
+    slabs_per_lane() = slabs_per_lane_;
+    return ok();
+}
+
 static int common_args(const float *lors, int64_t n, int32_t lor_stride, const void *image,
                        const int64_t *st, const void *image_t, const int64_t *st_t,
                        const int32_t grid[3], const float center[3], const float size[3], Grid &g,

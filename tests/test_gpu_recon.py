@@ -85,3 +85,23 @@ def test_osem_tof_matches_oracle(cuda_lib, oracle, small_case, emap_small, nsigm
                       tof=True, tof_bin=sc.tof.tof_bin, tof_sigma2=sc.tof.tof_sigma2,
                       tof_nsigma=nsigma)
     assert rel_l2(out.data, ref) <= TOL
+
+
+@pytest.mark.parametrize("lanes,spl", [(32, 2), (16, 4), (16, 2), (8, 4), (8, 2)])
+def test_osem_tuning_variants_match_oracle(cuda_lib, oracle, small_case, emap_small, lanes, spl):
+    import srf_gb300 as nef
+    from srf_gb300 import _lib
+    sc, ic, lors = small_case["scanner"], small_case["ic"], small_case["lors"]
+    lm = nef.Listmode(np.ones(len(lors), np.float32), nef.Lors(lors))
+    em = nef.Emap(emap_small, ic.center, ic.size)
+    _lib.set_tuning(lanes, spl)
+    try:
+        out = nef.OsemFullTof(1, 4, ic, sc, lm, em, tof_nsigma=3.0, seed=5)()
+    finally:
+        _lib.set_tuning(32, 4)
+    perm = np.random.default_rng(5).permutation(len(lors))
+    ref = oracle.osem(lors, lm.data, emap_small, ic.shape, ic.center, ic.size, 4, 4, perm,
+                      rule="full_tof", emap_scale=1.0 / 4, guard=True, subset_index="mod",
+                      tof=True, tof_bin=sc.tof.tof_bin, tof_sigma2=sc.tof.tof_sigma2,
+                      tof_nsigma=3.0)
+    assert rel_l2(out.data, ref) <= TOL
