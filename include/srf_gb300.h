@@ -173,6 +173,38 @@ int srf_osem_subset(const float *lors, int64_t n, int32_t lor_stride,
 int srf_osem_update(float *x, float *x_t, float *bp, float *bp_t, const float *emap,
                     int32_t guard_zero, const int32_t grid[3], void *stream);
 
+/* Many independent studies per launch (not in the reference). One descriptor per study, in
+ * DEVICE memory; images x/bp x-fastest ({1, nx, nx*ny}), x_t/bp_t y-fastest ({ny, 1, nx*ny}) or
+ * both NULL; emap (x-fastest) is read by srf_osem_update_batch. Descriptors cannot be checked on
+ * the host (no device-to-host copies); the kernels skip a study whose descriptor fails the
+ * host-side checks of srf_osem_subset (grid range, NULL pointers, stride). */
+typedef struct srf_study {
+    const float *lors;    /* this subset's LORs of the study */
+    int64_t n;
+    int32_t lor_stride;
+    int32_t tof_stride;   /* TOF values tof[i * tof_stride] (used when use_tof) */
+    const float *tof;
+    const float *y;       /* NULL: y_i = 1 */
+    float *x, *x_t, *bp, *bp_t;
+    const float *emap;
+    int32_t grid[3];
+    float center[3];
+    float size[3];
+} srf_study;
+
+/* srf_osem_subset for every study at once: a persistent kernel walks all studies' 32-LOR batches.
+ * batch_offsets (device, n_studies + 1): study s owns batches [off[s], off[s + 1]),
+ * off[s + 1] - off[s] = ceil(n_s / 32); total_batches = off[n_studies]. */
+int srf_osem_subset_batch(const srf_study *studies, int32_t n_studies,
+                          const int64_t *batch_offsets, int64_t total_batches, int32_t use_tof,
+                          float tof_bin, float tof_sigma2, float tof_nsigma, int32_t ratio_rule,
+                          float eps, double *loglik, void *stream);
+
+/* srf_osem_update for every study at once. tile_offsets (device, n_studies + 1): study s owns
+ * tiles [off[s], off[s + 1]), ceil(nx/32) * ceil(ny/32) * nz of them. */
+int srf_osem_update_batch(const srf_study *studies, int32_t n_studies, const int64_t *tile_offsets,
+                          int64_t total_tiles, int32_t guard_zero, void *stream);
+
 /* ------------------------------------------------------------------ sensitivity image */
 
 /* emap += sum over all ordered crystal pairs of the non-TOF backprojection of 1, generated on

@@ -119,6 +119,16 @@ inline int check_lors(const float *lors, int64_t n, int32_t stride) {
     return SRF_OK;
 }
 
+inline int check_tof_params(float tof_bin, float tof_sigma2, float tof_nsigma, TofParams &tp) {
+    if (!std::isfinite(tof_bin) || !std::isfinite(tof_sigma2) || !std::isfinite(tof_nsigma))
+        return fail(SRF_ENONFINITE, "non-finite TOF parameter");
+    if (tof_nsigma < 0) return fail(SRF_EINVAL, "tof_nsigma must be >= 0");
+    tp.tof_bin = tof_bin;
+    tp.tof_sigma2 = tof_sigma2;
+    tp.nsigma = tof_nsigma;
+    return SRF_OK;
+}
+
 inline int check_tof(const float *tof, int64_t n, int32_t tof_stride, float tof_bin, float tof_sigma2,
                      float tof_nsigma, TofParams &tp) {
     if (n > 0 && !tof) return fail(SRF_EINVAL, "tof must not be NULL");

@@ -205,34 +205,35 @@ __device__ __forceinline__ bool near_int(float t, float m) {
 // Relative margin on the TOF truncation test t2 <= nsigma^2 (fast t2 is within ~1e-5 relative).
 constexpr float kTruncMargin = 2e-4f;
 
-// Voxels of one slab from the (already floored) boundary coordinates: the branch-free form of the
-// reference's case analysis (siddon.cu.cc:86-189). w[c] == 0 marks a voxel that is not visited.
+// Voxels of one slab from the boundary coordinates: the branch-free form of the reference's case
+// analysis (siddon.cu.cc:86-189). With fq, fz the fractions of the slab before the q and z
+// crossings (1 when no crossing), the near corner (cq1, cz1) takes min(fq, fz), the far corner
+// (cq2, cz2) takes 1 - max of the crossings' fractions, and when both coordinates step the middle
+// voxel takes |fq - fz| ((cq1, cz2) if z steps first, else (cq2, cz1)). w[c] == 0 marks a voxel
+// that is not visited; the validity tests are the reference's range tests.
 __device__ __forceinline__ void slab_voxels(const LorRun &r, int ip, bool keep, float qq1, float qq2,
                                             float zz1, float zz2, float wt, int32_t o[3], float w[3]) {
     const int cq1 = ifloor(qq1), cq2 = ifloor(qq2);
     const int cz1 = ifloor(zz1), cz2 = ifloor(zz2);
     const bool dq = cq1 != cq2, dz = cz1 != cz2;
-    const bool R = keep && (dq ? (cq1 >= -1) : (cq1 >= 0)) && cq1 < r.nq &&
-                   (dz ? (cz1 >= -1) : (cz1 >= 0)) && cz1 < r.nz;
-    const float rq = dq ? __fdividef((float)cq2 - qq1, qq2 - qq1) : 0.0f;
-    const float rz = dz ? __fdividef((float)cz2 - zz1, zz2 - zz1) : 0.0f;
+    const bool R = keep && cq1 >= (dq ? -1 : 0) && cq1 < r.nq && cz1 >= (dz ? -1 : 0) && cz1 < r.nz;
+    const float fq = __fdividef((float)cq2 - qq1, qq2 - qq1);  // used only when dq
+    const float fz = __fdividef((float)cz2 - zz1, zz2 - zz1);  // used only when dz
+    const float f0 = fminf(dq ? fq : 1.0f, dz ? fz : 1.0f);
+    const float f2 = 1.0f - fmaxf(dq ? fq : 0.0f, dz ? fz : 0.0f);
     const int32_t base = ip * r.sp;
-    // near corner (cq1, cz1)
-    const bool v0 = R && cq1 >= 0 && cz1 >= 0;
-    const float f0 = dq ? (dz ? fminf(rq, rz) : rq) : (dz ? rz : 1.0f);
-    o[0] = v0 ? base + cq1 * r.sq + cz1 * r.szs : 0;
+    const int32_t q1o = cq1 * r.sq, q2o = cq2 * r.sq, z1o = cz1 * r.szs, z2o = cz2 * r.szs;
+    const bool v0 = R && (cq1 | cz1) >= 0;
+    const bool far_in = cq2 < r.nq && cz2 < r.nz;
+    const bool v2 = R && (dq || dz) && far_in;
+    const bool qfirst = fq > fz;
+    const bool v1 = R && dq && dz && (qfirst ? (cq1 >= 0 && cz2 < r.nz) : (cq2 < r.nq && cz1 >= 0));
+    o[0] = v0 ? base + q1o + z1o : 0;
     w[0] = v0 ? f0 * wt : 0.0f;
-    // far corner (cq2, cz2)
-    const bool v2 = R && (dq || dz) && cq2 < r.nq && cz2 < r.nz;
-    const float f2 = 1.0f - (dq ? (dz ? fmaxf(rq, rz) : rq) : rz);
-    o[2] = v2 ? base + cq2 * r.sq + cz2 * r.szs : 0;
+    o[2] = v2 ? base + q2o + z2o : 0;
     w[2] = v2 ? f2 * wt : 0.0f;
-    // middle voxel when both coordinates step: z first -> (cq1, cz2), else (cq2, cz1)
-    const bool qfirst = rq > rz;
-    const int mq = qfirst ? cq1 : cq2, mz = qfirst ? cz2 : cz1;
-    const bool v1 = R && dq && dz && mq >= 0 && mq < r.nq && mz >= 0 && mz < r.nz;
-    o[1] = v1 ? base + mq * r.sq + mz * r.szs : 0;
-    w[1] = v1 ? (qfirst ? (rq - rz) : (rz - rq)) * wt : 0.0f;
+    o[1] = v1 ? base + (qfirst ? q1o + z2o : q2o + z1o) : 0;
+    w[1] = v1 ? fabsf(fq - fz) * wt : 0.0f;
 }
 
 __device__ __forceinline__ bool proj_slab_rule(const LorRun &r, bool tof, float pp1, float pp2) {

@@ -48,11 +48,120 @@ __device__ __forceinline__ void chunk_candidates(const LorRun &run, const GridK 
     for (int u = 0; u < U; ++u) {
         const int ip = c0 + lane + G * u;
         const bool act = ip <= run.hi;
-        candidates_fast<TOF>(run, k, act ? ip : run.hi, act, o[u], w[u], pm[u], bad[u]);
+        if (c0 + G * u <= run.hi) {  // uniform over the group: skip slots past the range
+            candidates_fast<TOF>(run, k, act ? ip : run.hi, act, o[u], w[u], pm[u], bad[u]);
+        } else {
+            o[u][0] = o[u][1] = o[u][2] = 0;
+            w[u][0] = w[u][1] = w[u][2] = 0.0f;
+            pm[u] = false;
+            bad[u] = false;
+        }
     }
 #pragma unroll
     for (int u = 0; u < U; ++u)
         if (bad[u]) candidates_exact<TOF>(run, k, c0 + lane + G * u, o[u], w[u], pm[u]);
+}
+
+// LORs [base, base + 32) of one study: lane-parallel setup of the 32 records into wrecs, then
+// the warp's 32/G groups walk them (projection, ratio, backprojection per LOR). x/x_t and
+// bp/bp_t have equal strides (offsets are computed once for the gather and the scatter).
+template <int G, bool TOF, int U>
+__device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__restrict__ lors,
+                                                int64_t n, int stride, const float *__restrict__ tof,
+                                                int tof_stride, const Grid &g, const GridK &k,
+                                                const TofParams &tp, const float *__restrict__ y,
+                                                int rule, float eps, const View &x, const View &xt,
+                                                const View &bp, const View &bpt, int64_t base,
+                                                bool want_ll, double &ll) {
+    constexpr int GPW = 32 / G;
+    const int lane32 = threadIdx.x & 31;
+    const int lane = threadIdx.x & (G - 1);
+    const int gi = lane32 / G;
+    const bool have_t = xt.ptr != nullptr;
+    {  // lane-parallel setup of the warp's next 32 LORs
+        const int64_t i = base + lane32;
+        LorRec R = {};
+        R.lo = 1;
+        if (i < n) {
+            const float *l = lors + i * stride;
+            float lv[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
+            const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
+            const float yv = y ? __ldg(y + i) : 1.0f;
+            R = setup_rec<TOF>(lv, tv, yv, g, k);
+        }
+        store_rec(&wrecs[lane32], R);
+    }
+    __syncwarp();
+    for (int j0 = 0; j0 < 32; j0 += GPW) {
+        const int j = j0 + gi;
+        const LorRec R = load_rec(&wrecs[j]);
+        const int64_t i = base + j;
+        if (R.flags & F_TIE) {
+            float lv[6];
+            const float *l = lors + i * stride;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
+            const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
+            tie_path<G, TOF>(lv, tv, R.yv, lane, g, tp, x, xt, bp, bpt, rule, eps, ll, want_ll);
+            continue;
+        }
+        const bool valid = R.flags & F_VALID;
+        const LorRun run = make_run(R, g, k, x.st, xt.st, have_t);
+        const float *xim = (!run.xdom && have_t) ? xt.ptr : x.ptr;
+        float *bim = (!run.xdom && have_t) ? bpt.ptr : bp.ptr;
+        const bool proj_ok = R.flags & F_PROJ;
+        const bool single = (run.hi - run.lo + 1) <= G * U;
+        int32_t o[U][3];
+        float w[U][3];
+        bool pm[U];
+        float acc = 0.0f;
+        if (valid) {
+            for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
+                chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
+                if (proj_ok) {
+                    float xv[U][3];
+#pragma unroll
+                    for (int u = 0; u < U; ++u)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c)
+                            xv[u][c] = (pm[u] && w[u][c] != 0.0f) ? __ldg(xim + o[u][c]) : 0.0f;
+#pragma unroll
+                    for (int u = 0; u < U; ++u)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) acc = fmaf(xv[u][c], w[u][c], acc);
+                }
+            }
+        }
+        const float p = group_sum<G>(acc) * R.invL2;
+        if (!valid) continue;
+        const float den = __fadd_rn(p, eps);
+        float r;
+        if (rule == SRF_RATIO_DIV_NO_NAN)
+            r = (den == 0.0f) ? 0.0f : __fdiv_rn(R.yv, den);
+        else
+            r = __fdiv_rn(R.yv, den);
+        if (want_ll && lane == 0 && den > 0.0f) ll += (double)R.yv * (double)__logf(den);
+        if (r == 0.0f) continue;
+        if (single) {
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    if (w[u][c] != 0.0f) atomicAdd(bim + o[u][c], r * w[u][c]);
+        } else {
+            for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
+                chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                        if (w[u][c] != 0.0f) atomicAdd(bim + o[u][c], r * w[u][c]);
+            }
+        }
+    }
+    __syncwarp();
 }
 
 // One warp handles 32 consecutive LORs per round: lane j sets up LOR j into shared memory, then
@@ -63,103 +172,16 @@ __global__ void __launch_bounds__(kBlock, MINB)
 k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
               int tof_stride, Grid g, TofParams tp, const float *__restrict__ y, int rule, float eps,
               View x, View xt, View bp, View bpt, double *__restrict__ loglik) {
-    constexpr int GPW = 32 / G;
     __shared__ LorRec recs[kBlock / 32][32];
     const int wib = threadIdx.x >> 5;
     const int lane32 = threadIdx.x & 31;
-    const int lane = threadIdx.x & (G - 1);
-    const int gi = lane32 / G;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const GridK k = make_gridk<TOF>(g, tp);
-    const bool have_t = xt.ptr != nullptr;
     const bool want_ll = loglik != nullptr;
     double ll = 0.0;
     for (int64_t base = warp * 32; base < n; base += nwarps * 32) {
-        {  // lane-parallel setup of the warp's next 32 LORs
-            const int64_t i = base + lane32;
-            LorRec R = {};
-            R.lo = 1;
-            if (i < n) {
-                const float *l = lors + i * stride;
-                float lv[6];
-#pragma unroll
-                for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
-                const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
-                const float yv = y ? __ldg(y + i) : 1.0f;
-                R = setup_rec<TOF>(lv, tv, yv, g, k);
-            }
-            store_rec(&recs[wib][lane32], R);
-        }
-        __syncwarp();
-        for (int j0 = 0; j0 < 32; j0 += GPW) {
-            const int j = j0 + gi;
-            const LorRec R = load_rec(&recs[wib][j]);
-            const int64_t i = base + j;
-            if (R.flags & F_TIE) {
-                float lv[6];
-                const float *l = lors + i * stride;
-#pragma unroll
-                for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
-                const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
-                tie_path<G, TOF>(lv, tv, R.yv, lane, g, tp, x, xt, bp, bpt, rule, eps, ll, want_ll);
-                continue;
-            }
-            const bool valid = R.flags & F_VALID;
-            const LorRun run = make_run(R, g, k, x.st, xt.st, have_t);
-            const float *xim = (!run.xdom && have_t) ? xt.ptr : x.ptr;
-            float *bim = (!run.xdom && have_t) ? bpt.ptr : bp.ptr;
-            const bool proj_ok = R.flags & F_PROJ;
-            const bool single = (run.hi - run.lo + 1) <= G * U;
-            int32_t o[U][3];
-            float w[U][3];
-            bool pm[U];
-            float acc = 0.0f;
-            if (valid) {
-                for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
-                    chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
-                    if (proj_ok) {
-                        float xv[U][3];
-#pragma unroll
-                        for (int u = 0; u < U; ++u)
-#pragma unroll
-                            for (int c = 0; c < 3; ++c)
-                                xv[u][c] = (pm[u] && w[u][c] != 0.0f) ? __ldg(xim + o[u][c]) : 0.0f;
-#pragma unroll
-                        for (int u = 0; u < U; ++u)
-#pragma unroll
-                            for (int c = 0; c < 3; ++c) acc = fmaf(xv[u][c], w[u][c], acc);
-                    }
-                }
-            }
-            const float p = group_sum<G>(acc) * R.invL2;
-            if (!valid) continue;
-            const float den = __fadd_rn(p, eps);
-            float r;
-            if (rule == SRF_RATIO_DIV_NO_NAN)
-                r = (den == 0.0f) ? 0.0f : __fdiv_rn(R.yv, den);
-            else
-                r = __fdiv_rn(R.yv, den);
-            if (want_ll && lane == 0 && den > 0.0f) ll += (double)R.yv * (double)__logf(den);
-            if (r == 0.0f) continue;
-            if (single) {
-#pragma unroll
-                for (int u = 0; u < U; ++u)
-#pragma unroll
-                    for (int c = 0; c < 3; ++c)
-                        if (w[u][c] != 0.0f) atomicAdd(bim + o[u][c], r * w[u][c]);
-            } else {
-                for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
-                    chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
-#pragma unroll
-                    for (int u = 0; u < U; ++u)
-#pragma unroll
-                        for (int c = 0; c < 3; ++c)
-                            if (w[u][c] != 0.0f) atomicAdd(bim + o[u][c], r * w[u][c]);
-                }
-            }
-        }
-        __syncwarp();
+        osem_warp_batch<G, TOF, U>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, y, rule, eps, x, xt, bp, bpt, base, want_ll, ll);
     }
     if (want_ll) {
 #pragma unroll
@@ -204,37 +226,52 @@ static int launch_osem(const float *lors, int64_t n, int stride, const float *to
 // 32 x 32 (x, y) tiles of one z slice; 32 x 8 threads.
 constexpr int kTile = 32;
 
-__global__ void __launch_bounds__(kTile * 8)
-k_osem_update(float *__restrict__ x, float *__restrict__ xt, float *__restrict__ bp,
-              float *__restrict__ bpt, const float *__restrict__ emap, int guard, int nx, int ny) {
-    __shared__ float tin[kTile][kTile + 1];
-    __shared__ float tout[kTile][kTile + 1];
-    const int bx = blockIdx.x * kTile, by = blockIdx.y * kTile;
-    const int64_t zoff = (int64_t)blockIdx.z * nx * ny;
+// One 32 x 32 (x, y) tile of z slice bz; 32 x 8 threads.
+__device__ __forceinline__ void update_tile(float *__restrict__ x, float *__restrict__ xt,
+                                            float *__restrict__ bp, float *__restrict__ bpt,
+                                            const float *__restrict__ emap, int guard, int nx,
+                                            int ny, int tbx, int tby, int bz,
+                                            float (&tin)[kTile][kTile + 1],
+                                            float (&tout)[kTile][kTile + 1]) {
+    constexpr int R = kTile / 8;  // rows per thread
+    const int bx = tbx * kTile, by = tby * kTile;
+    const int64_t zoff = (int64_t)bz * nx * ny;
     const int tx = threadIdx.x, ty = threadIdx.y;
+    // issue every load of this thread before any store, so a thread has 4R loads in flight
+    float vb[R], vx[R], ve[R], vt[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int iy = by + ty + 8 * r, ix = bx + tx;
+        const bool in = ix < nx && iy < ny;
+        const int64_t o = zoff + (int64_t)iy * nx + ix;
+        vb[r] = in ? bp[o] : 0.0f;
+        vx[r] = in ? x[o] : 0.0f;
+        ve[r] = in ? emap[o] : 1.0f;
+        if (bpt) {  // bpt is y-fastest: element (ix, iy) at ix*ny + iy
+            const int jx = bx + ty + 8 * r, jy = by + tx;
+            vt[r] = (jx < nx && jy < ny) ? bpt[zoff + (int64_t)jx * ny + jy] : 0.0f;
+        }
+    }
     if (bpt) {
-        // bpt is y-fastest: element (ix, iy) at ix*ny + iy
-        for (int j = ty; j < kTile; j += 8) {
-            const int ix = bx + j, iy = by + tx;
-            float v = 0.0f;
-            if (ix < nx && iy < ny) {
-                const int64_t o = zoff + (int64_t)ix * ny + iy;
-                v = bpt[o];
-                bpt[o] = 0.0f;
-            }
-            tin[j][tx] = v;  // [x_local][y_local]
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int jx = bx + ty + 8 * r, jy = by + tx;
+            tin[ty + 8 * r][tx] = vt[r];  // [x_local][y_local]
+            if (jx < nx && jy < ny) bpt[zoff + (int64_t)jx * ny + jy] = 0.0f;
         }
         __syncthreads();
     }
-    for (int j = ty; j < kTile; j += 8) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int j = ty + 8 * r;
         const int iy = by + j, ix = bx + tx;
         if (ix < nx && iy < ny) {
             const int64_t o = zoff + (int64_t)iy * nx + ix;
-            float b = bp[o];
+            float b = vb[r];
             if (bpt) b = __fadd_rn(b, tin[tx][j]);
-            float e = emap[o];
+            float e = ve[r];
             if (guard && e == 0.0f) e = 1e8f;
-            const float xn = __fdiv_rn(__fmul_rn(x[o], b), e);
+            const float xn = __fdiv_rn(__fmul_rn(vx[r], b), e);
             x[o] = xn;
             bp[o] = 0.0f;
             tout[j][tx] = xn;  // [y_local][x_local]
@@ -242,10 +279,119 @@ k_osem_update(float *__restrict__ x, float *__restrict__ xt, float *__restrict__
     }
     if (xt) {
         __syncthreads();
-        for (int j = ty; j < kTile; j += 8) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int j = ty + 8 * r;
             const int ix = bx + j, iy = by + tx;
             if (ix < nx && iy < ny) xt[zoff + (int64_t)ix * ny + iy] = tout[tx][j];
         }
+    }
+}
+
+
+__global__ void __launch_bounds__(kTile * 8)
+k_osem_update(float *__restrict__ x, float *__restrict__ xt, float *__restrict__ bp,
+              float *__restrict__ bpt, const float *__restrict__ emap, int guard, int nx, int ny) {
+    __shared__ float tin[kTile][kTile + 1];
+    __shared__ float tout[kTile][kTile + 1];
+    update_tile(x, xt, bp, bpt, emap, guard, nx, ny, blockIdx.x, blockIdx.y, blockIdx.z, tin, tout);
+}
+
+// ---------------------------------------------------------------- many studies per launch
+
+// Index of the segment holding `v` in an ascending offsets array off[0..n] (off[0] = 0).
+__device__ __forceinline__ int find_segment(const int64_t *__restrict__ off, int n, int64_t v) {
+    int lo = 0, hi = n;  // invariant: off[lo] <= v < off[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ bool study_ok(const srf_study &st) {
+    return st.n >= 0 && st.lor_stride >= 6 && st.grid[0] > 0 && st.grid[1] > 0 && st.grid[2] > 0 &&
+           st.grid[0] <= 65536 && st.grid[1] <= 65536 && st.grid[2] <= 65536 &&
+           (int64_t)st.grid[0] * st.grid[1] * st.grid[2] < (int64_t(1) << 31) && st.lors &&
+           st.x && st.bp && st.size[0] > 0.0f && st.size[1] > 0.0f && st.size[2] > 0.0f &&
+           ((st.x_t == nullptr) == (st.bp_t == nullptr));
+}
+
+// Persistent kernel over all studies' LOR batches: warp-batch b belongs to the study s with
+// boff[s] <= b < boff[s + 1] (32 LORs per batch, each study padded to whole batches).
+template <int G, bool TOF, int U, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB)
+k_osem_batch(const srf_study *__restrict__ studies, int n_studies, const int64_t *__restrict__ boff,
+             int64_t total_batches, TofParams tp, int rule, float eps, double *__restrict__ loglik) {
+    __shared__ LorRec recs[kBlock / 32][32];
+    const int wib = threadIdx.x >> 5;
+    const int lane32 = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool want_ll = loglik != nullptr;
+    double ll = 0.0;
+    for (int64_t b = warp; b < total_batches; b += nwarps) {
+        const int s = find_segment(boff, n_studies, b);
+        const srf_study st = studies[s];
+        if (!study_ok(st)) continue;  // uniform over the warp
+        if (TOF && (st.tof == nullptr || st.tof_stride < 1)) continue;
+        const Grid g{st.grid[0], st.grid[1], st.grid[2], st.center[0], st.center[1], st.center[2],
+                     st.size[0], st.size[1], st.size[2]};
+        const GridK k = make_gridk<TOF>(g, tp);
+        const int64_t nxy = (int64_t)g.nx * g.ny;
+        const View x{st.x, {1, g.nx, nxy}}, bp{st.bp, {1, g.nx, nxy}};
+        const View xt{st.x_t, {g.ny, 1, nxy}}, bpt{st.bp_t, {g.ny, 1, nxy}};
+        const int64_t base = (b - __ldg(boff + s)) * 32;
+        osem_warp_batch<G, TOF, U>(recs[wib], st.lors, st.n, st.lor_stride, st.tof, st.tof_stride,
+                                   g, k, tp, st.y, rule, eps, x, xt, bp, bpt, base, want_ll, ll);
+    }
+    if (want_ll) {
+#pragma unroll
+        for (int o2 = 16; o2 > 0; o2 >>= 1) ll += __shfl_xor_sync(0xffffffffu, ll, o2);
+        if (lane32 == 0 && ll != 0.0) atomicAdd(loglik, ll);
+    }
+}
+
+// Update of all studies: block t belongs to study s with toff[s] <= t < toff[s + 1].
+__global__ void __launch_bounds__(kTile * 8)
+k_osem_update_batch(const srf_study *__restrict__ studies, int n_studies,
+                    const int64_t *__restrict__ toff, int guard) {
+    __shared__ float tin[kTile][kTile + 1];
+    __shared__ float tout[kTile][kTile + 1];
+    const int64_t t = blockIdx.x;
+    const int s = find_segment(toff, n_studies, t);
+    const srf_study st = studies[s];
+    if (!study_ok(st) || st.emap == nullptr) return;  // uniform over the block
+    const int tx = (st.grid[0] + kTile - 1) / kTile, ty = (st.grid[1] + kTile - 1) / kTile;
+    const int64_t local = t - __ldg(toff + s);
+    if (local >= (int64_t)tx * ty * st.grid[2]) return;
+    const int bz = (int)(local / ((int64_t)tx * ty));
+    const int rem = (int)(local - (int64_t)bz * tx * ty);
+    update_tile(st.x, st.x_t, st.bp, st.bp_t, st.emap, guard, st.grid[0], st.grid[1], rem % tx,
+                rem / tx, bz, tin, tout);
+}
+
+template <int G, bool TOF, int U, int MINB>
+static int launch_batch_g(const srf_study *studies, int n_studies, const int64_t *boff,
+                          int64_t total, const TofParams &tp, int rule, float eps, double *ll,
+                          cudaStream_t s) {
+    auto kern = k_osem_batch<G, TOF, U, MINB>;
+    unsigned blocks = grid_for(kern, total * 32, kBlock);
+    kern<<<blocks, kBlock, 0, s>>>(studies, n_studies, boff, total, tp, rule, eps, ll);
+    return check_cuda("osem batch kernel launch");
+}
+
+template <bool TOF>
+static int launch_batch(const srf_study *studies, int n_studies, const int64_t *boff, int64_t total,
+                        const TofParams &tp, int rule, float eps, double *ll, cudaStream_t s) {
+    const int u = slabs_per_lane();
+    switch (group_lanes()) {
+    case 8: return u == 2 ? launch_batch_g<8, TOF, 2, 3>(studies, n_studies, boff, total, tp, rule, eps, ll, s)
+                          : launch_batch_g<8, TOF, 4, 2>(studies, n_studies, boff, total, tp, rule, eps, ll, s);
+    case 16: return u == 2 ? launch_batch_g<16, TOF, 2, 3>(studies, n_studies, boff, total, tp, rule, eps, ll, s)
+                           : launch_batch_g<16, TOF, 4, 2>(studies, n_studies, boff, total, tp, rule, eps, ll, s);
+    default: return u == 2 ? launch_batch_g<32, TOF, 2, 3>(studies, n_studies, boff, total, tp, rule, eps, ll, s)
+                           : launch_batch_g<32, TOF, 4, 2>(studies, n_studies, boff, total, tp, rule, eps, ll, s);
     }
 }
 
@@ -254,6 +400,39 @@ k_osem_update(float *__restrict__ x, float *__restrict__ xt, float *__restrict__
 using namespace srf;
 
 extern "C" {
+
+int srf_osem_subset_batch(const srf_study *studies, int32_t n_studies,
+                          const int64_t *batch_offsets, int64_t total_batches, int32_t use_tof,
+                          float tof_bin, float tof_sigma2, float tof_nsigma, int32_t ratio_rule,
+                          float eps, double *loglik, void *stream) {
+    if (n_studies < 0 || total_batches < 0) return fail(SRF_EINVAL, "negative counts");
+    if (n_studies == 0 || total_batches == 0) return ok();
+    if (!studies || !batch_offsets) return fail(SRF_EINVAL, "studies and batch_offsets must not be NULL");
+    if (ratio_rule != SRF_RATIO_DIV_NO_NAN && ratio_rule != SRF_RATIO_PLAIN)
+        return fail(SRF_EINVAL, "unknown ratio rule %d", ratio_rule);
+    if (!std::isfinite(eps)) return fail(SRF_ENONFINITE, "eps is not finite");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (use_tof) {
+        TofParams tp;
+        int rc;
+        if ((rc = check_tof_params(tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
+        return launch_batch<true>(studies, n_studies, batch_offsets, total_batches, tp, ratio_rule, eps, loglik, s);
+    }
+    TofParams tp{0, 0, 0};
+    return launch_batch<false>(studies, n_studies, batch_offsets, total_batches, tp, ratio_rule, eps, loglik, s);
+}
+
+int srf_osem_update_batch(const srf_study *studies, int32_t n_studies, const int64_t *tile_offsets,
+                          int64_t total_tiles, int32_t guard_zero, void *stream) {
+    if (n_studies < 0 || total_tiles < 0) return fail(SRF_EINVAL, "negative counts");
+    if (n_studies == 0 || total_tiles == 0) return ok();
+    if (!studies || !tile_offsets) return fail(SRF_EINVAL, "studies and tile_offsets must not be NULL");
+    if (total_tiles > 0x7fffffffLL) return fail(SRF_ERANGE, "too many tiles");
+    k_osem_update_batch<<<(unsigned)total_tiles, dim3(kTile, 8), 0, (cudaStream_t)stream>>>(
+        studies, n_studies, tile_offsets, guard_zero);
+    return check_cuda("osem update batch kernel launch");
+}
+
 
 int srf_osem_subset(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
                     int32_t tof_stride, float tof_bin, float tof_sigma2, float tof_nsigma,
