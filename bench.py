@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -51,6 +52,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=20250101)
+    ap.add_argument("--workload", default="clinical", choices=["clinical", "batched", "components"],
+                    help="clinical: the TOF OSEM headline; batched: 64 uneven studies; "
+                         "components: every kernel of the path against the CPU oracle")
+    ap.add_argument("--studies", type=int, default=64)
+    ap.add_argument("--autotune", action="store_true", help="tune lanes/slabs per lane first")
     return ap.parse_args()
 
 
@@ -228,11 +234,247 @@ def run_reference(a, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(a, ws, rank, local):
+    """64 independent TOF studies (events log-uniform in [1e5, 5e6], images 64^3, 96x96x64,
+    128x128x80 or 160x160x80 at 2, 3 or 4 mm), 4 subsets x 2 iterations each, on the clinical
+    scanner: every study alone (two kernels per subset step) and all studies together (two batch
+    kernels per subset step, one iteration captured in a CUDA graph and replayed)."""
+    import numpy as np
+    import torch
+    from srf_gb300 import _lib, autotune, kernels, synth
+    from srf_gb300._lib import SRF_RATIO_DIV_NO_NAN
+    from srf_gb300.geometry import ImageConfig, block_full_crystal_table
+    from srf_gb300.studies import Study, StudyBatch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.load()
+    sc = synth.scanner_clinical()
+    tof = (sc.tof.tof_bin, sc.tof.tof_sigma2)
+    rng = np.random.default_rng(a.seed + 17 * rank)
+    shapes = [(64, 64, 64), (96, 96, 64), (128, 128, 80), (160, 160, 80)]
+    n_sub, n_iter = 4, 2
+    table = torch.as_tensor(block_full_crystal_table(sc), device=dev)
+    emaps = {}
+    studies, meta = [], []
+    t0 = time.perf_counter()
+    for j in range(a.studies):
+        shape = shapes[int(rng.integers(0, 4))]
+        vox = float(rng.choice([2.0, 3.0, 4.0]))
+        n = int(round(math.exp(rng.uniform(math.log(1e5), math.log(5e6)))))
+        ic = ImageConfig(list(shape), [0.0, 0.0, 0.0], [s * vox for s in shape])
+        key = (shape, vox)
+        if key not in emaps:
+            emaps[key] = kernels.emap_block_full(table, sc.nb_blocks_per_ring, ic.shape, ic.center, ic.size)
+        act = synth.phantom_body(ic, seed=a.seed + j, device=dev)
+        lors = synth.sample_events(sc, ic, act, n, seed=a.seed + 1000 + j, tof_fwhm_ps=530.0, device=dev)
+        emx = kernels.xfast(emaps[key] / n_sub)
+        studies.append(Study(lors, ic.shape, ic.center, ic.size, emx))
+        meta.append({"shape": list(shape), "voxel_mm": vox, "events": n})
+    setup_s = time.perf_counter() - t0
+    tuned = None
+    if a.autotune:
+        big = max(range(len(studies)), key=lambda j: studies[j].lors.shape[0])
+        s0 = studies[big]
+        tuned = autotune.tune(s0.lors[: 1 << 20].contiguous(), s0.shape, s0.center, s0.size, tof,
+                              a.nsigma, reps=2, cache=None)
+    batch = StudyBatch(studies, n_sub, tof, tof_nsigma=a.nsigma, seed=a.seed)
+    visits = []
+    for st in studies:
+        f = kernels.count_pairs(st.lors, st.shape, st.center, st.size, rules=0, tof=tof, tof_nsigma=a.nsigma)
+        b = kernels.count_pairs(st.lors, st.shape, st.center, st.size, rules=1, tof=tof, tof_nsigma=a.nsigma)
+        visits.append(f + b)
+    stream = torch.cuda.current_stream(dev)
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    # every study alone
+    per_study = []
+    for st in studies:
+        per = st.lors.shape[0] // n_sub
+
+        def one_iter():
+            for k in range(n_sub):
+                st.state.subset(st.lors[k * per:(k + 1) * per], None, rule=SRF_RATIO_DIV_NO_NAN,
+                                eps=1e-5, tof=tof, tof_nsigma=a.nsigma)
+                st.state.update(st.emap, guard_zero=True)
+        one_iter()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        for _ in range(n_iter):
+            one_iter()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        per_study.append(e0.elapsed_time(e1) / n_iter / 1000.0)
+    # all together: eager, then graph replay
+    batch.reset()
+    batch.iteration()
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(n_iter):
+        batch.iteration()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    eager_s = e0.elapsed_time(e1) / n_iter / 1000.0
+    batch.reset()
+    batch.capture()
+    batch.reset()
+    clocks = Clocks(local)
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(max(a.steps, n_iter)):
+        batch.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    graph_s = e0.elapsed_time(e1) / max(a.steps, n_iter) / 1000.0
+    total_visits = float(sum(visits))
+    if rank == 0:
+        line = {
+            "metric": "batched TOF OSEM s/iter (64 uneven studies) & LOR-voxel updates/s",
+            "value": total_visits / graph_s, "unit": UNIT, "n_gpus": ws, "steps": max(a.steps, n_iter),
+            "warmup": 1, "ms_per_step": graph_s * 1000.0, "s_per_iter_all_studies": graph_s,
+            "s_per_iter_all_studies_eager_batch": eager_s,
+            "s_per_iter_sum_of_single_studies": float(sum(per_study)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded phantoms per study)",
+            "config": {"workload": "batched_uneven_studies", "studies": len(studies),
+                       "subsets": n_sub, "iterations": n_iter, "tof_nsigma": a.nsigma,
+                       "events_total": int(sum(m["events"] for m in meta)),
+                       "setup_s": setup_s, "autotune": tuned},
+            "per_study": [dict(m, s_per_iter=t, visits_per_iter=v) for m, t, v in zip(meta, per_study, visits)],
+            "gpu_launches": 2 * n_sub * max(a.steps, n_iter), "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def run_components(a, ws, rank, local):
+    """Each kernel of the path on the clinical geometry, timed with CUDA events (best of 5 after
+    a warm-up), beside the CPU oracle on a sample (single thread)."""
+    import numpy as np
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from srf_gb300 import _lib, kernels, synth
+    from srf_gb300.geometry import block_full_crystal_table, EcatIndexToCrystalPos
+    from srf_gb300._lib import SRF_RATIO_DIV_NO_NAN
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.load()
+    O.build()
+    sc, ic = synth.scanner_clinical(), synth.image_clinical()
+    act = synth.phantom_body(ic, seed=a.seed + 7, device=dev)
+    n = 2_000_000
+    lors = synth.sample_events(sc, ic, act, n, seed=a.seed, tof_fwhm_ps=530.0, device=dev)
+    lors6 = lors[:, :6].contiguous()
+    tof = (sc.tof.tof_bin, sc.tof.tof_sigma2)
+    img = kernels.xfast(act + 0.1)
+    img_t = kernels.yfast(img)
+    vals = torch.rand(n, device=dev)
+    samp = 20000
+    l_np, l6_np = lors[:samp].cpu().numpy(), lors6[:samp].cpu().numpy()
+    img_np = img.contiguous().cpu().numpy()
+    v_np = vals[:samp].cpu().numpy()
+
+    def gpu_ms(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    def cpu_s(fn):
+        t0 = time.perf_counter()
+        fn()
+        return time.perf_counter() - t0
+
+    out = {}
+    for name, t, rules, ns in (("projection_tof_3sigma", tof, 0, a.nsigma), ("backprojection_tof_3sigma", tof, 1, a.nsigma),
+                               ("projection_tof_exact", tof, 0, 0.0), ("backprojection_tof_exact", tof, 1, 0.0),
+                               ("projection_nontof", None, 0, 0.0), ("backprojection_nontof", None, 1, 0.0)):
+        L = lors if t is not None else lors6
+        pairs = kernels.count_pairs(L, ic.shape, ic.center, ic.size, rules=rules, tof=t, tof_nsigma=ns)
+        if rules == 0:
+            ms = gpu_ms(lambda: kernels.project(L, img, ic.center, ic.size, tof=t, tof_nsigma=ns, image_t=img_t))
+        else:
+            ms = gpu_ms(lambda: kernels.backproject(L, vals, ic.shape, ic.center, ic.size, tof=t, tof_nsigma=ns))
+        kw = dict(tof=True, tof_bin=t[0], tof_sigma2=t[1], tof_nsigma=ns) if t is not None else {}
+        Ln = l_np if t is not None else l6_np
+        if rules == 0:
+            cs = cpu_s(lambda: O.projection(img_np, Ln, ic.shape, ic.center, ic.size, **kw))
+        else:
+            cs = cpu_s(lambda: O.backprojection(v_np, Ln, ic.shape, ic.center, ic.size, **kw))
+        cpu_pairs = pairs * samp / n
+        out[name] = {"lors": n, "pairs": pairs, "ms": ms, "pairs_per_s": pairs / (ms / 1e3),
+                     "cpu_pairs_per_s": cpu_pairs / cs, "cpu_sample_lors": samp}
+    st = kernels.SubsetState(ic.shape, ic.center, ic.size, dev)
+    ms = gpu_ms(lambda: st.subset(lors, None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5, tof=tof, tof_nsigma=a.nsigma))
+    pf = out["projection_tof_3sigma"]["pairs"] + out["backprojection_tof_3sigma"]["pairs"]
+    out["osem_subset_fused"] = {"lors": n, "pairs": pf, "ms": ms, "pairs_per_s": pf / (ms / 1e3)}
+    em_x = kernels.xfast(torch.ones(ic.shape, device=dev))
+    ms = gpu_ms(lambda: st.update(em_x, guard_zero=True))
+    out["osem_update"] = {"voxels": int(np.prod(ic.shape)), "ms": ms,
+                          "gb_per_s": 8 * 4 * float(np.prod(ic.shape)) / (ms / 1e3) / 1e9}
+    table = torch.as_tensor(block_full_crystal_table(sc), device=dev)
+    ms = gpu_ms(lambda: kernels.emap_block_full(table, sc.nb_blocks_per_ring, ic.shape, ic.center, ic.size), reps=2)
+    m = table.shape[0] // sc.nb_blocks_per_ring
+    tnp = table.cpu().numpy()
+    p1 = np.repeat(tnp[:m][:40], m, axis=0)
+    p2 = np.tile(tnp[5 * m:6 * m], (40, 1))
+    cl = np.hstack([p1, p2]).astype(np.float32)
+    cs = cpu_s(lambda: O.backprojection(np.ones(len(cl), np.float32), cl, ic.shape, ic.center, ic.size))
+    out["emap_block_full"] = {"lors": int(sc.nb_crystals) ** 2, "ms": ms,
+                              "lors_per_s": sc.nb_crystals ** 2 / (ms / 1e3), "cpu_lors_per_s": len(cl) / cs}
+    # single-scatter simulation: random crystal pairs x scatter points of a 64x64x32 volume
+    rng = np.random.default_rng(a.seed)
+    cpos = EcatIndexToCrystalPos(sc)(np.arange(sc.nb_crystals)).astype(np.float32)
+    n_s = 12 * 12 * 4
+    spos = np.stack(np.meshgrid(np.linspace(-250, 250, 12), np.linspace(-250, 250, 12),
+                                np.linspace(-80, 80, 4), indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    em = rng.uniform(0.5, 2.0, (sc.nb_crystals, n_s)).astype(np.float32)
+    at = rng.uniform(0.2, 1.0, (sc.nb_crystals, n_s)).astype(np.float32)
+    umap = (rng.random((64, 64, 32)) * 0.0096).astype(np.float32)
+    np_pairs = 200_000
+    pairs = rng.integers(0, sc.nb_crystals, (np_pairs, 2)).astype(np.int32)
+    d = lambda x: torch.as_tensor(x).to(dev)
+    args = (d(cpos), d(spos), d(em), d(at), d(umap), [600.0, 600.0, 208.0], 624, 48, [1, 13, 13], 350, 650, 0.15)
+    ms = gpu_ms(lambda: kernels.sss(d(pairs), *args), reps=3)
+    cs = cpu_s(lambda: O.sss(pairs[:2000], cpos, spos, em, at, umap, [600.0, 600.0, 208.0], 624, 48, [1, 13, 13], 350, 650, 0.15))
+    out["sss"] = {"pairs": np_pairs, "scatter_points": n_s, "ms": ms,
+                  "evals_per_s": np_pairs * n_s / (ms / 1e3), "cpu_evals_per_s": 2000 * n_s / cs}
+    ms = gpu_ms(lambda: kernels.snap(lors, sc))
+    from srf_gb300.geometry import PetEcatListmodeTrans
+    from srf_gb300.data import Listmode, Lors
+    cs = cpu_s(lambda: PetEcatListmodeTrans(sc)(Listmode(np.ones(samp, np.float32), Lors(l_np))))
+    out["listmode_snap"] = {"events": n, "ms": ms, "events_per_s": n / (ms / 1e3), "cpu_events_per_s": samp / cs}
+    ms = gpu_ms(lambda: kernels.lm2sino(lors, None, sc))
+    out["lm2sino"] = {"events": n, "ms": ms, "events_per_s": n / (ms / 1e3)}
+    mu = kernels.xfast(act * 0.0096)
+    ms = gpu_ms(lambda: kernels.attenuation(lors6, mu, ic.center, ic.size))
+    out["attenuation_fused"] = {"lors": n, "ms": ms, "lors_per_s": n / (ms / 1e3)}
+    if rank == 0:
+        print(json.dumps({"metric": "per-kernel throughput, clinical geometry", "workload": "components",
+                          "components": out, "cpu_threads": 1, "data": "synthetic"}), flush=True)
+
+
 def main():
     a = parse()
     ws, rank, local = dist_setup(a)
     if a.impl == "reference":
         run_reference(a, ws, rank)
+        return
+    if a.workload == "batched":
+        run_batched(a, ws, rank, local)
+        return
+    if a.workload == "components":
+        run_components(a, ws, rank, local)
         return
     import numpy as np
     import torch

@@ -205,6 +205,36 @@ int srf_osem_subset_batch(const srf_study *studies, int32_t n_studies,
 int srf_osem_update_batch(const srf_study *studies, int32_t n_studies, const int64_t *tile_offsets,
                           int64_t total_tiles, int32_t guard_zero, void *stream);
 
+/* ------------------------------------------------------------------ list-mode ingestion */
+
+/* Scanner description for the list-mode kernels (PetEcatScanner, srfnef/geometry/pet_ecat_scanner.py):
+ *   scanner[8]       = {average_radius, angle_per_block, axial_length, gap, block_size_y,
+ *                       block_size_z, unit_size_y, unit_size_z}
+ *   scanner_shape[4] = {block_shape_y, block_shape_z, nb_blocks_per_ring, nb_rings} */
+
+/* Crystal ids of both endpoints (crystal_ids[2i], [2i+1], optional) and/or the LORs with both
+ * endpoints snapped to crystal centres (out, out_stride floats per row; columns past 6 copied,
+ * e.g. the TOF value). EcatCrystalPosToIndex + EcatIndexToCrystalPos + PetEcatListmodeTrans
+ * (srfnef/functions/geometry/pet_ecat_scanner.py:15-89, functions/data_transform/pet_ecat.py:43-60). */
+int srf_listmode_snap(const float *lors, int64_t n, int32_t lor_stride, const double scanner[8],
+                      const int64_t scanner_shape[4], float *out, int32_t out_stride,
+                      int64_t *crystal_ids, void *stream);
+
+/* sino[bin] += values[i] (1 when NULL) with bin = (hi - 1) * hi / 2 + lo of the ordered crystal
+ * pair: lm2sino / cal_sinogram (srfnef/corrections/scattering/listmode2sinogram.py:17-23, 76-85).
+ * sino: float64, n_bins = n_crystals (n_crystals - 1) / 2. Events whose bin falls outside are
+ * counted in *dropped (device, optional). */
+int srf_lm2sino(const float *lors, int64_t n, int32_t lor_stride, const float *values,
+                const double scanner[8], const int64_t scanner_shape[4], double *sino,
+                int64_t n_bins, unsigned long long *dropped, void *stream);
+
+/* out[i] = exp(-(P mu)_i * L_i^2 / (size[0] / grid[0])) (UmapProject, attenuation_correct.py:31-40),
+ * or, with values != NULL, out[i] = values[i] / exp(-(...)) (AttenuationCorrect, :16-28): the
+ * non-TOF projection of the mu map and its epilogue in one pass. */
+int srf_attenuation(const float *lors, int64_t n, int32_t lor_stride, const float *umap,
+                    const int64_t umap_strides[3], const int32_t grid[3], const float center[3],
+                    const float size[3], const float *values, float *out, void *stream);
+
 /* ------------------------------------------------------------------ sensitivity image */
 
 /* emap += sum over all ordered crystal pairs of the non-TOF backprojection of 1, generated on

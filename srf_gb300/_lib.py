@@ -27,7 +27,7 @@ EXPORTS = (
     "srf_projection_tof", "srf_backprojection_tof", "srf_projection_adjoint", "srf_fold_views",
     "srf_copy_view", "srf_count_pairs", "srf_osem_subset", "srf_osem_update", "srf_osem_subset_batch",
     "srf_osem_update_batch", "srf_emap_block_full", "srf_sss",
-    "srf_backprojection_tof_noalloc",
+    "srf_backprojection_tof_noalloc", "srf_listmode_snap", "srf_lm2sino", "srf_attenuation",
 )
 
 

@@ -4,7 +4,7 @@
 
 namespace srf {
 
-enum Action : int { GATHER = 0, SCATTER = 1, COUNT = 2 };
+enum Action : int { GATHER = 0, SCATTER = 1, COUNT = 2, ATTEN = 3 };
 
 // Warp-uniform loop over LORs: each warp takes 32/G consecutive LORs per round, so the group
 // shuffles in group_sum always see all 32 lanes.
@@ -34,7 +34,7 @@ k_trace(const float *__restrict__ lors, int64_t n, int stride, const float *__re
                 if (ACTION == COUNT) {
                     for (int ip = S.lo + lane; ip <= S.hi; ip += G)
                         slab<TOF, RULES>(S, ip, [&](int32_t, float) { acc += 1.0f; });
-                } else if (ACTION == GATHER) {
+                } else if (ACTION == GATHER || ACTION == ATTEN) {
                     const float *imc = im;
                     for (int ip = S.lo + lane; ip <= S.hi; ip += G)
                         slab<TOF, RULES>(S, ip, [&](int32_t off, float w) { acc += __ldg(imc + off) * w; });
@@ -49,6 +49,19 @@ k_trace(const float *__restrict__ lors, int64_t n, int stride, const float *__re
         if (ACTION == GATHER) {
             acc = group_sum<G>(acc);
             if (valid && lane == 0) out[i] = acc;
+        } else if (ACTION == ATTEN) {
+            // UmapProject epilogue: exp(-(p * L * L / unit)), L from the raw endpoints in FP32
+            acc = group_sum<G>(acc);
+            if (valid && lane == 0) {
+                const float *l = lors + i * stride;
+                const float dx = __fsub_rn(__ldg(l), __ldg(l + 3)), dy = __fsub_rn(__ldg(l + 1), __ldg(l + 4));
+                const float dz = __fsub_rn(__ldg(l + 2), __ldg(l + 5));
+                const float L = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+                const float unit = __fdiv_rn(g.sx, (float)g.nx);
+                const float v = __fdiv_rn(__fmul_rn(__fmul_rn(acc, L), L), unit);
+                const float a = expf(-v);
+                out[i] = values ? __fdiv_rn(__ldg(values + i), a) : a;
+            }
         } else if (ACTION == COUNT) {
             acc = group_sum<G>(acc);  // < 2^24 visits per LOR, exact in FP32
             if (valid && lane == 0 && acc > 0.0f)
@@ -223,6 +236,16 @@ int srf_count_pairs(const float *lors, int64_t n, int32_t lor_stride, const floa
     return rules == RULES_PROJ
                ? launch_trace<false, RULES_PROJ, COUNT>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, nullptr, out, s)
                : launch_trace<false, RULES_BACK, COUNT>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, nullptr, out, s);
+}
+
+int srf_attenuation(const float *lors, int64_t n, int32_t lor_stride, const float *umap,
+                    const int64_t umap_strides[3], const int32_t grid[3], const float center[3],
+                    const float size[3], const float *values, float *out, void *stream) {
+    Grid g; View v, vt; int rc;
+    if ((rc = common_args(lors, n, lor_stride, umap, umap_strides, nullptr, nullptr, grid, center, size, g, v, vt))) return rc;
+    if (n > 0 && !out) return fail(SRF_EINVAL, "out must not be NULL");
+    TofParams tp{0, 0, 0};
+    return launch_trace<false, RULES_PROJ, ATTEN>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, values, out, (cudaStream_t)stream);
 }
 
 static int elementwise_args(const void *dst, const int64_t *ds, const void *src, const int64_t *ss,

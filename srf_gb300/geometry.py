@@ -141,6 +141,14 @@ class PetEcatListmodeTrans(_NefLike):
     scanner: Optional[PetEcatScanner] = None
 
     def __call__(self, listmode: Listmode) -> Listmode:
+        try:
+            import torch
+            on_gpu = isinstance(listmode.lors.data, torch.Tensor) and listmode.lors.data.is_cuda
+        except ImportError:  # pragma: no cover
+            on_gpu = False
+        if on_gpu:  # one GPU pass (srf_listmode_snap)
+            from . import kernels
+            return listmode.update(lors=Lors(kernels.snap(listmode.lors.data.contiguous(), self.scanner)))
         lors = np.asarray(listmode.lors.data)
         ind1 = EcatCrystalPosToIndex(self.scanner)(lors[:, :3])
         ind2 = EcatCrystalPosToIndex(self.scanner)(lors[:, 3:6])

@@ -208,3 +208,55 @@ def sss(pairs: torch.Tensor, crystal_pos: torch.Tensor, scatter_pos: torch.Tenso
          i32x3(grid_block), i32(low_energy), i32(high_energy), f32(resolution), ptr(scatter),
          ptr(scale), stream_ptr(dev))
     return scatter, scale
+
+
+# ---------------------------------------------------------------- list-mode ingestion
+
+def scanner_args(scanner):
+    """(double[8], int64[4]) description of a PetEcatScanner for the list-mode kernels."""
+    import ctypes
+    b = scanner.blocks
+    d = (ctypes.c_double * 8)(scanner.average_radius, scanner.angle_per_block, scanner.axial_length,
+                              scanner.gap, b.size[1], b.size[2], b.unit_size[1], b.unit_size[2])
+    s = (ctypes.c_int64 * 4)(int(b.shape[1]), int(b.shape[2]), int(scanner.nb_blocks_per_ring),
+                             int(scanner.nb_rings))
+    return d, s
+
+
+def snap(lors: torch.Tensor, scanner, want_ids: bool = False):
+    """Endpoints snapped to crystal centres (columns past 6 kept); optionally the crystal ids."""
+    _require_cuda(lors, "lors")
+    n, stride = lors.shape[0], lors.stride(0)
+    out = torch.empty_like(lors)
+    ids = torch.empty((n, 2), dtype=torch.int64, device=lors.device) if want_ids else None
+    d, s = scanner_args(scanner)
+    call("srf_listmode_snap", ptr(lors), i64(n), i32(stride), d, s, ptr(out), i32(out.stride(0)),
+         ptr(ids), stream_ptr(lors.device))
+    return (out, ids) if want_ids else out
+
+
+def lm2sino(lors: torch.Tensor, values: Optional[torch.Tensor], scanner) -> Tuple[torch.Tensor, int]:
+    """Triangular crystal-pair sinogram (float64, n(n-1)/2 bins) and the number of dropped events."""
+    _require_cuda(lors, "lors")
+    nc = scanner.nb_crystals
+    sino = torch.zeros(nc * (nc - 1) // 2, dtype=torch.float64, device=lors.device)
+    dropped = torch.zeros(1, dtype=torch.int64, device=lors.device)
+    d, s = scanner_args(scanner)
+    call("srf_lm2sino", ptr(lors), i64(lors.shape[0]), i32(lors.stride(0)),
+         ptr(values.contiguous() if values is not None else None), d, s, ptr(sino), i64(sino.numel()),
+         ptr(dropped), stream_ptr(lors.device))
+    return sino, int(dropped.item())
+
+
+def attenuation(lors: torch.Tensor, umap: torch.Tensor, center, size,
+                values: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """exp(-(P mu) L^2 / unit) per LOR, or values / that (AttenuationCorrect) when values given."""
+    n, stride = check_lors(lors, False)
+    _require_cuda(umap, "umap")
+    if umap.stride(0) != 1:
+        umap = xfast(umap)
+    out = torch.empty(n, dtype=F32, device=lors.device)
+    call("srf_attenuation", ptr(lors), i64(n), i32(stride), ptr(umap), i64x3(umap.stride()),
+         i32x3(umap.shape), f32x3(center), f32x3(size),
+         ptr(values.contiguous() if values is not None else None), ptr(out), stream_ptr(lors.device))
+    return out

@@ -49,14 +49,18 @@ def _lor_lengths(lors: np.ndarray) -> np.ndarray:
     return np.sqrt(dx ** 2 + dy ** 2 + dz ** 2)
 
 
+def _back(t: torch.Tensor, like):
+    return t if isinstance(like, torch.Tensor) else t.cpu().numpy()
+
+
 @dataclasses.dataclass(frozen=True)
 class UmapProject(_NefLike):
+    """One fused GPU pass (srf_attenuation): projection of mu and exp(-p L^2 / unit)."""
+
     def __call__(self, u_map: Image, lors: Lors) -> Listmode:
-        lors_np = np.asarray(lors.data, dtype=np.float32)
-        proj = Project("tf-eager")(u_map.update(data=np.asarray(u_map.data, np.float32)), lors)
-        L = _lor_lengths(lors_np)
-        val = proj.data * L * L / u_map.unit_size[0]
-        return Listmode(np.exp(-val), lors)
+        lt = to_dev(lors.data).contiguous()
+        a = kernels.attenuation(lt, to_dev(u_map.data), list(u_map.center), list(u_map.size))
+        return Listmode(_back(a, lors.data), lors)
 
 
 @dataclasses.dataclass(frozen=True)
@@ -64,12 +68,10 @@ class AttenuationCorrect(_NefLike):
     u_map: Optional[Umap] = None
 
     def __call__(self, listmode: Listmode) -> Listmode:
-        lors_np = np.asarray(listmode.lors.data, dtype=np.float32)
-        proj = Project("tf-eager")(self.u_map.update(data=np.asarray(self.u_map.data, np.float32)),
-                                   listmode.lors)
-        L = _lor_lengths(lors_np)
-        val = proj.data * L * L / self.u_map.unit_size[0]
-        return listmode.update(data=np.asarray(listmode.data) / np.exp(-val))
+        lt = to_dev(listmode.lors.data).contiguous()
+        y = kernels.attenuation(lt, to_dev(self.u_map.data), list(self.u_map.center),
+                                list(self.u_map.size), values=to_dev(listmode.data))
+        return listmode.update(data=_back(y, listmode.data))
 
 
 # ------------------------------------------------------------------ sinogram formats

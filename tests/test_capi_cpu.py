@@ -78,3 +78,24 @@ def test_argument_checks(lib):
     assert b"ratio" in lib.srf_last_error()
     # empty input succeeds without a launch
     assert p(None, ctypes.c_int64(0), 6, fake, st, None, None, grid, center, size, None, None) == 0
+
+
+def test_study_descriptor_layout_matches_header(tmp_path):
+    """srf_gb300.studies.SrfStudy (ctypes) must lay out exactly like the C srf_study."""
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    from srf_gb300.studies import SrfStudy
+    src = tmp_path / "sz.cc"
+    src.write_text('#include <cstdio>\n#include <cstddef>\n#include "srf_gb300.h"\n'
+                   'int main(){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(srf_study),'
+                   ' offsetof(srf_study, n), offsetof(srf_study, emap), offsetof(srf_study, grid),'
+                   ' offsetof(srf_study, center), offsetof(srf_study, size));}\n')
+    exe = tmp_path / "sz"
+    subprocess.run([cxx, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    want = [ctypes.sizeof(SrfStudy), SrfStudy.n.offset, SrfStudy.emap.offset, SrfStudy.grid.offset,
+            SrfStudy.center.offset, SrfStudy.size.offset]
+    assert [int(v) for v in got] == want
