@@ -52,9 +52,13 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=20250101)
-    ap.add_argument("--workload", default="clinical", choices=["clinical", "batched", "components"],
+    ap.add_argument("--workload", default="clinical",
+                    choices=["clinical", "batched", "components", "surrogate", "profile"],
                     help="clinical: the TOF OSEM headline; batched: 64 uneven studies; "
-                         "components: every kernel of the path against the CPU oracle")
+                         "components: every kernel of the path against the CPU oracle; "
+                         "surrogate: learned scatter estimate against SSS (time, sinogram and "
+                         "OSEM image agreement); profile: subset steps only, the case ncu captures")
+    ap.add_argument("--held-out", type=int, default=20, help="surrogate: held-out phantoms timed")
     ap.add_argument("--studies", type=int, default=64)
     ap.add_argument("--autotune", action="store_true", help="tune lanes/slabs per lane first")
     return ap.parse_args()
@@ -464,6 +468,107 @@ def run_components(a, ws, rank, local):
                           "components": out, "cpu_threads": 1, "data": "synthetic"}), flush=True)
 
 
+def run_profile(a, ws, rank, local):
+    """Subset steps of the clinical workload without the sensitivity image and visit counts
+    (emap = 1): warmup + steps iterations of n_subsets (subset, update) launch pairs."""
+    import torch
+    from srf_gb300 import _lib, kernels
+    from srf_gb300._lib import SRF_RATIO_DIV_NO_NAN
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.load()
+    _lib.set_group_lanes(a.lanes)
+    sc, ic, act, lors = make_workload(a, dev, rank)
+    tof = (sc.tof.tof_bin, sc.tof.tof_sigma2)
+    n_per = lors.shape[0] // a.subsets
+    em = torch.ones(ic.shape[::-1], device=dev).permute(2, 1, 0)
+    st = kernels.SubsetState(ic.shape, ic.center, ic.size, dev)
+    for _ in range(a.warmup + a.steps):
+        for k in range(a.subsets):
+            st.subset(lors[k * n_per:(k + 1) * n_per], None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5,
+                      tof=tof, tof_nsigma=a.nsigma)
+            st.update(em, guard_zero=True)
+    torch.cuda.synchronize()
+    if rank == 0:
+        print(json.dumps({"workload": "profile", "events": int(lors.shape[0]), "lors_per_launch": n_per,
+                          "subset_launches": (a.warmup + a.steps) * a.subsets}), flush=True)
+
+
+def run_surrogate(a, ws, rank, local):
+    """Learned scatter estimate against the single-scatter simulation on held-out phantoms.
+
+    Scatter estimation time, from the emission and mu volumes to the coarse scatter sinogram:
+    SSS = preprocessing projections + srf_sss over all 827,424 bins; surrogate = network input
+    projections + U-Net forward + trilinear upsampling + the spot-check SSS on 2048 random bins.
+    Agreement: full-sinogram relative L2 on every held-out phantom, and for one study the TOF
+    OSEM image with the surrogate's scatter against the image with SSS scatter (and the image
+    without scatter correction, for scale)."""
+    import torch
+    from srf_gb300 import _lib, synth
+    from srf_gb300.scatter_sinogram import CoarseGeometry, ScatterStudy, random_phantom, sss_sinogram
+    from srf_gb300.surrogate import ScatterSurrogate
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.load()
+    geo = CoarseGeometry(synth.scanner_clinical(), device=dev)
+    sur = ScatterSurrogate.load(geo)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(f):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        r = f()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return max(e0.elapsed_time(e1) / 1000.0, time.perf_counter() - t0), r
+
+    seeds = [1_000_000 + i for i in range(a.held_out)]
+    em, mu = random_phantom(seeds[0], device=dev)
+    for _ in range(max(a.warmup, 1)):
+        sss_sinogram(geo, em, mu)
+        sur.estimate(em, mu)
+    t_sss, t_sur, errs, spot, fallbacks = [], [], [], [], 0
+    clocks = Clocks(local)
+    for sd in seeds:
+        em, mu = random_phantom(sd, device=dev)
+        ts, ref = timed(lambda: sss_sinogram(geo, em, mu))
+        tc, (est, info) = timed(lambda: sur.estimate(em, mu))
+        pred = sur.predict(em, mu)
+        errs.append(float((torch.linalg.vector_norm(pred - ref) / torch.linalg.vector_norm(ref)).item()))
+        spot.append(info["spot_rel_l2"])
+        fallbacks += int(info["fallback"])
+        t_sss.append(ts)
+        t_sur.append(tc)
+    clk = clocks.stop()
+    study = ScatterStudy(geo, seeds[0], n_trues=int(min(a.events, 2e6)))
+    img_sss = study.reconstruct(study.sss)
+    img_sur = study.reconstruct(sur.predict(study.emission, study.mu))
+    rel = lambda u, v: float((torch.linalg.vector_norm(u - v) / torch.linalg.vector_norm(v)).item())
+    med_sss, med_sur = statistics.median(t_sss), statistics.median(t_sur)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "scatter estimation speed-up of the learned surrogate over SSS (same sinogram)",
+            "value": med_sss / med_sur, "unit": "x", "n_gpus": ws, "steps": len(seeds),
+            "warmup": max(a.warmup, 1), "ms_per_step": 1000 * med_sur, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (network), f32 (SSS)",
+            "data": "synthetic (seeded held-out phantoms)",
+            "config": {"workload": "scatter_surrogate", "volumes": [64, 64, 32], "bins": geo.n_bins(),
+                       "scatter_points": int(geo.scatter_points.shape[0]), "held_out": len(seeds),
+                       "spot_check_bins": sur.spot_bins, "fallback_tol": sur.fallback_tol,
+                       "params": sur.net.n_params()},
+            "sss_s_median": med_sss, "surrogate_s_median": med_sur,
+            "sinogram_rel_l2_mean": sum(errs) / len(errs), "sinogram_rel_l2_max": max(errs),
+            "spot_rel_l2_mean": sum(spot) / len(spot), "fallbacks": fallbacks,
+            "osem": {"events": int(study.events.shape[0]), "scatter_fraction": study.sf,
+                     "iterations": study.n_iter, "subsets": study.n_sub,
+                     "image_rel_l2_surrogate_vs_sss": rel(img_sur, img_sss),
+                     "image_rel_l2_uncorrected_vs_sss": rel(study.x0, img_sss)},
+            "clocks": clk,
+        }), flush=True)
+
+
 def main():
     a = parse()
     ws, rank, local = dist_setup(a)
@@ -475,6 +580,12 @@ def main():
         return
     if a.workload == "components":
         run_components(a, ws, rank, local)
+        return
+    if a.workload == "surrogate":
+        run_surrogate(a, ws, rank, local)
+        return
+    if a.workload == "profile":
+        run_profile(a, ws, rank, local)
         return
     import numpy as np
     import torch

@@ -151,18 +151,19 @@ int srf_copy_view(float *dst, const int64_t dst_strides[3], const float *src,
 #define SRF_RATIO_PLAIN 1
 
 /* One fused subset step of list-mode MLEM/OSEM for the LORs given:
- *   p_i = (A x)_i ; r_i = rule(y_i, p_i) ; bp += A_bp^T r
+ *   p_i = (A x)_i ; r_i = rule(y_i, p_i + add_i) ; bp += A_bp^T r
  * in a single pass over the LORs (each LOR's projection, ratio and backprojection are computed
  * back to back; p and r never reach memory). tof == NULL: non-TOF projector/backprojector pair of
  * srf_projection/srf_backprojection; otherwise the TOF pair. y == NULL means y_i = 1 (list mode).
  * x/x_t are read (x_t optional, y-fastest), bp/bp_t accumulate (bp_t optional, folded by
- * srf_osem_update). loglik (optional, device double) += sum_i y_i * log(p_i + eps).
+ * srf_osem_update). add (optional) is an additive expected count per LOR, e.g. a scatter estimate
+ * (not in the reference; NULL = 0). loglik (optional, device double) += sum_i y_i log(p_i + add_i + eps).
  * Replaces the per-iteration bodies of mlem_full.py:66-70, mlem_full_tof.py:62-67,
  * mlem.py:39-43 and osem_full.py:74-77 up to the image update. */
 int srf_osem_subset(const float *lors, int64_t n, int32_t lor_stride,
                     const float *tof, int32_t tof_stride,
                     float tof_bin, float tof_sigma2, float tof_nsigma,
-                    const float *y, int32_t ratio_rule, float eps,
+                    const float *y, const float *add, int32_t ratio_rule, float eps,
                     const float *x, const float *x_t, float *bp, float *bp_t,
                     const int32_t grid[3], const float center[3], const float size[3],
                     double *loglik, void *stream);
@@ -265,6 +266,46 @@ int srf_sss(const int32_t *pairs, int64_t n_pairs, const float *crystal_pos, int
             const float umap_size[3], int32_t nb_crystals_per_ring, int32_t nb_blocks_per_ring,
             const int32_t grid_block[3], int32_t low_energy, int32_t high_energy,
             float resolution, float *scatter, float *scale, void *stream);
+
+/* ------------------------------------------------------------------ scatter surrogate network */
+/* BF16 3-D U-Net building blocks with FP32 accumulation (not in the reference). Activations are
+ * NDHWC bfloat16 described by int32[6] = {n, d, h, w, channel_stride, channel_offset} so a layer
+ * reads or writes a channel slice of a wider buffer. Weights are [Cout][27][Cin] bfloat16. */
+
+/* y = act(b + conv3x3x3(x, w)), pad 1; relu != 0 applies max(., 0). Cin, Cout multiples of 16.
+ * yf (optional) receives the FP32 values. Runs on the tensor cores (mma.sync BF16). */
+int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *w, const float *bias,
+                   int32_t cout, int32_t relu, void *y, const int32_t ys[6], float *yf, void *stream);
+/* dw[co][tap][ci] += sum_v dy[v, co] x[v + tap - 1, ci] (FP32 accumulation). */
+int srf_conv3d_wgrad(const void *x, const int32_t xs[6], int32_t cin, const void *dy, const int32_t ds[6],
+                     int32_t cout, float *dw, void *stream);
+/* wf[ci][26 - tap][co] = w[co][tap][ci]: weights of the data-gradient convolution. */
+int srf_conv3d_flip_weights(const void *w, int32_t cout, int32_t cin, void *wf, void *stream);
+/* g = 0 where y <= 0 (ReLU backward from the layer output). */
+int srf_cnn_relu_bwd(void *g, const int32_t gs[6], const void *y, const int32_t ys[6], int32_t c, void *stream);
+/* db[c] += sum_v g[v, c]. */
+int srf_cnn_bias_grad(const void *g, const int32_t gs[6], int32_t c, float *db, void *stream);
+/* 2x2x2 average pooling fine -> coarse (adjoint: coarse gradient -> fine gradient). */
+int srf_cnn_pool2(const void *fine, const int32_t fs[6], void *coarse, const int32_t cs[6], int32_t c,
+                  int32_t adjoint, void *stream);
+/* nearest 2x upsampling coarse -> fine (adjoint: fine gradient summed into coarse). */
+int srf_cnn_upsample2(const void *coarse, const int32_t cs[6], void *fine, const int32_t fs[6], int32_t c,
+                      int32_t adjoint, void *stream);
+/* dst slice += src slice. */
+int srf_cnn_add(void *dst, const int32_t ds[6], const void *src, const int32_t ss[6], int32_t c, void *stream);
+/* 1x1x1 head to one FP32 channel: forward when gout == NULL, else gradients (gx, gw, gb). */
+int srf_cnn_head(const void *x, const int32_t xs[6], int32_t c, const float *w, const float *b, float *out,
+                 const float *gout, void *gx, const int32_t gs[6], float *gw, float *gb, void *stream);
+/* *loss += (1/n_samples) sum_s sum_i m (p - t)^2 inv_den[s] (FP64); grad = its gradient,
+   2 m (p - t) inv_den[s] / n_samples. */
+int srf_cnn_rel_mse(const float *pred, const float *target, const float *mask, const float *inv_den,
+                    int64_t per_sample, int32_t n_samples, float *grad, double *loss, void *stream);
+/* trilinear 2x upsampling of single-channel FP32 volumes (n, d, h, w) -> (n, D, H, W). */
+int srf_cnn_trilinear2(const float *src, int32_t n, int32_t d, int32_t h, int32_t w, float *dst, int32_t D,
+                       int32_t H, int32_t W, void *stream);
+/* Adam step on FP32 parameters, refreshing an optional BF16 copy. */
+int srf_cnn_adam(float *w, float *m, float *v, const float *g, void *bf16_copy, int64_t n, float lr,
+                 float b1, float b2, float eps, int32_t step, void *stream);
 
 #ifdef __cplusplus
 }

@@ -248,7 +248,7 @@ def osem_subsets(n, n_sub, perm):
 
 def osem(lors, values, emap, shape, center, size, n_iter, n_sub, perm, *, rule="full_tof",
          emap_scale=1.0, guard=True, subset_index="mod", tof=False, tof_bin=0.0, tof_sigma2=0.0,
-         tof_nsigma=0.0, x0=None):
+         tof_nsigma=0.0, x0=None, add=None):
     """OSEM: per step i the subset is i // n_sub ('reference' literal, osem_full.py:68) or
     i % n_sub ('mod'); n_iter counts subset steps as in the reference loop. The emap is the full
     sensitivity times emap_scale, zero-guarded when guard=True."""
@@ -264,6 +264,8 @@ def osem(lors, values, emap, shape, center, size, n_iter, n_sub, perm, *, rule="
         idx = subs[k]
         sl = np.ascontiguousarray(lors[idx])
         p = projection(x, sl, shape, center, size, **kw)
+        if add is not None:
+            p = (p + np.asarray(add, np.float32)[idx]).astype(np.float32)
         r = ratio(y[idx], p, rule)
         bp = backprojection(r, sl, shape, center, size, **kw)
         x = (x * bp / em).astype(np.float32)

@@ -1,0 +1,577 @@
+// BF16 3-D convolution network kernels with FP32 accumulation (scatter surrogate; not in the
+// reference).
+//
+// Activations are NDHWC bfloat16 with an explicit channel stride and offset, so a layer can
+// read or write a channel slice of a wider buffer (U-Net skip concatenation costs nothing).
+// Weights are [Cout][27][Cin] bfloat16 (tap-major within an output channel), FP32 master copies
+// live in the optimiser.
+//
+// conv3d 3x3x3 (pad 1, stride 1) is an implicit GEMM: rows = output voxels, columns = output
+// channels, K = 27 taps x Cin. A CTA of 4 warps computes a 64-voxel x 64-channel tile; for each
+// (tap, 16-channel chunk) the gathered input rows (zero outside the volume) and the weight slice
+// are staged in shared memory and each warp issues 8 mma.sync.m16n8k16 BF16 tensor-core
+// products into FP32 accumulators. The data gradient is the same kernel on flipped, transposed
+// weights. The weight gradient is a split-K GEMM over voxels per tap, accumulated with FP32
+// atomics. Requirements (checked on the host): Cin and Cout multiples of 16, channel strides and
+// offsets multiples of 8 (16-byte aligned rows).
+#include <algorithm>
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace srf {
+
+constexpr int kCM = 64, kCN = 64, kCK = 16, kCPad = 24;  // tile sizes, padded smem row (bf16)
+
+struct Act {  // NDHWC view
+    int n, d, h, w, cstride, coff;
+};
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ uint32_t lds32(const __nv_bfloat16 *p) {
+    return *reinterpret_cast<const uint32_t *>(p);
+}
+
+// One k-step of a warp: A rows [r0, r0+16) of As, B columns [0, 64) of Bs (stored [n][k]).
+__device__ __forceinline__ void warp_mma_step(const __nv_bfloat16 (*As)[kCPad],
+                                              const __nv_bfloat16 (*Bs)[kCPad], int r0,
+                                              float (&acc)[8][4]) {
+    const int lane = threadIdx.x & 31, grp = lane >> 2, tig = lane & 3;
+    uint32_t a[4];
+    a[0] = lds32(&As[r0 + grp][tig * 2]);
+    a[1] = lds32(&As[r0 + grp + 8][tig * 2]);
+    a[2] = lds32(&As[r0 + grp][tig * 2 + 8]);
+    a[3] = lds32(&As[r0 + grp + 8][tig * 2 + 8]);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        uint32_t b[2];
+        b[0] = lds32(&Bs[j * 8 + grp][tig * 2]);
+        b[1] = lds32(&Bs[j * 8 + grp][tig * 2 + 8]);
+        mma_bf16(acc[j], a, b);
+    }
+}
+
+// y[v, co] = act(b[co] + sum_{tap, ci} x[v + tap - 1, ci] w[co, tap, ci])
+__global__ void __launch_bounds__(128)
+k_conv3d_fwd(const __nv_bfloat16 *__restrict__ x, Act xa, int cin, const __nv_bfloat16 *__restrict__ wt,
+             const float *__restrict__ bias, int cout, int relu, __nv_bfloat16 *__restrict__ y, Act ya,
+             float *__restrict__ yf) {
+    __shared__ __align__(16) __nv_bfloat16 As[kCM][kCPad];
+    __shared__ __align__(16) __nv_bfloat16 Bs[kCN][kCPad];
+    const int64_t nvox = (int64_t)xa.d * xa.h * xa.w;
+    const int64_t v0 = (int64_t)blockIdx.x * kCM;
+    const int co0 = blockIdx.y * kCN;
+    const int nb = blockIdx.z;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    float acc[8][4] = {};
+    // loader role: thread t loads half a row (8 channels) of A and of B
+    const int lr = tid >> 1, lh = (tid & 1) * 8;
+    const int64_t lv = v0 + lr;
+    const bool lv_ok = lv < nvox;
+    const int lz = lv_ok ? (int)(lv / ((int64_t)xa.h * xa.w)) : 0;
+    const int lrem = lv_ok ? (int)(lv - (int64_t)lz * xa.h * xa.w) : 0;
+    const int ly = lrem / xa.w, lx = lrem - ly * xa.w;
+    const __nv_bfloat16 *xb = x + (int64_t)nb * nvox * xa.cstride + xa.coff;
+    const int lco = co0 + lr;
+    for (int tap = 0; tap < 27; ++tap) {
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+        const int zz = lz + dz, yy = ly + dy, xx = lx + dx;
+        const bool in = lv_ok && zz >= 0 && zz < xa.d && yy >= 0 && yy < xa.h && xx >= 0 && xx < xa.w;
+        const int64_t src = in ? (((int64_t)zz * xa.h + yy) * xa.w + xx) * xa.cstride : 0;
+        for (int c0 = 0; c0 < cin; c0 += kCK) {
+            uint4 av = make_uint4(0, 0, 0, 0), bv = make_uint4(0, 0, 0, 0);
+            if (in) av = *reinterpret_cast<const uint4 *>(xb + src + c0 + lh);
+            if (lco < cout) bv = *reinterpret_cast<const uint4 *>(wt + ((int64_t)lco * 27 + tap) * cin + c0 + lh);
+            *reinterpret_cast<uint4 *>(&As[lr][lh]) = av;
+            *reinterpret_cast<uint4 *>(&Bs[lr][lh]) = bv;
+            __syncthreads();
+            warp_mma_step(As, Bs, warp * 16, acc);
+            __syncthreads();
+        }
+    }
+    // epilogue: rows (warp*16 + grp, +8), columns (j*8 + tig*2, +1)
+    const int lane = tid & 31, grp = lane >> 2, tig = lane & 3;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int co = co0 + j * 8 + tig * 2;
+        if (co >= cout) continue;
+        const float b0 = bias ? bias[co] : 0.0f, b1 = bias ? bias[co + 1] : 0.0f;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int64_t v = v0 + warp * 16 + grp + half * 8;
+            if (v >= nvox) continue;
+            float r0 = acc[j][half * 2] + b0, r1 = acc[j][half * 2 + 1] + b1;
+            if (relu) {
+                r0 = fmaxf(r0, 0.0f);
+                r1 = fmaxf(r1, 0.0f);
+            }
+            const int64_t o = ((int64_t)nb * nvox + v) * ya.cstride + ya.coff + co;
+            *reinterpret_cast<__nv_bfloat162 *>(y + o) = __floats2bfloat162_rn(r0, r1);
+            if (yf) {
+                yf[o] = r0;
+                yf[o + 1] = r1;
+            }
+        }
+    }
+}
+
+// dw[co, tap, ci] += sum_v dy[v, co] x[v + tap - 1, ci]; grid (voxel splits, 27 taps, co/ci tiles)
+__global__ void __launch_bounds__(128)
+k_conv3d_wgrad(const __nv_bfloat16 *__restrict__ x, Act xa, int cin, const __nv_bfloat16 *__restrict__ dy,
+               Act da, int cout, float *__restrict__ dw, int64_t vox_per_split) {
+    __shared__ __align__(16) __nv_bfloat16 As[kCM][kCPad];  // [co][v]
+    __shared__ __align__(16) __nv_bfloat16 Bs[kCN][kCPad];  // [ci][v]
+    const int64_t nvox = (int64_t)xa.d * xa.h * xa.w;
+    const int64_t total = nvox * xa.n;
+    const int tap = blockIdx.y;
+    const int dz = tap / 9 - 1, dyo = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+    const int ci_tiles = (cin + kCN - 1) / kCN;
+    const int co0 = (blockIdx.z / ci_tiles) * kCM, ci0 = (blockIdx.z % ci_tiles) * kCN;
+    const int64_t vbeg = (int64_t)blockIdx.x * vox_per_split;
+    const int64_t vend = min(total, vbeg + vox_per_split);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    float acc[8][4] = {};
+    // loader role: thread t handles voxel (t & 15) of the chunk and an 8-channel group (t >> 4)
+    const int lvv = tid & 15, lg = tid >> 4;  // lg in [0, 8): channels lg*8 .. lg*8+7
+    for (int64_t vc = vbeg; vc < vend; vc += kCK) {
+        const int64_t v = vc + lvv;
+        __nv_bfloat16 da8[8], xa8[8];
+        bool vok = v < vend;
+        int64_t nb = 0, lv = 0;
+        if (vok) {
+            nb = v / nvox;
+            lv = v - nb * nvox;
+        }
+        // dy row (v, co0 + lg*8 ..)
+        {
+            uint4 t = make_uint4(0, 0, 0, 0);
+            if (vok && co0 + lg * 8 < cout)
+                t = *reinterpret_cast<const uint4 *>(dy + (nb * nvox + lv) * da.cstride + da.coff + co0 + lg * 8);
+            *reinterpret_cast<uint4 *>(da8) = t;
+        }
+        // shifted x row (v + tap - 1, ci0 + lg*8 ..)
+        {
+            uint4 t = make_uint4(0, 0, 0, 0);
+            if (vok) {
+                const int z = (int)(lv / ((int64_t)xa.h * xa.w));
+                const int rem = (int)(lv - (int64_t)z * xa.h * xa.w);
+                const int yy = rem / xa.w + dyo, xx = rem % xa.w + dx, zz = z + dz;
+                if (zz >= 0 && zz < xa.d && yy >= 0 && yy < xa.h && xx >= 0 && xx < xa.w && ci0 + lg * 8 < cin)
+                    t = *reinterpret_cast<const uint4 *>(
+                        x + ((nb * nvox) + ((int64_t)zz * xa.h + yy) * xa.w + xx) * xa.cstride + xa.coff + ci0 + lg * 8);
+            }
+            *reinterpret_cast<uint4 *>(xa8) = t;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            As[lg * 8 + j][lvv] = da8[j];
+            Bs[lg * 8 + j][lvv] = xa8[j];
+        }
+        __syncthreads();
+        warp_mma_step(As, Bs, warp * 16, acc);
+        __syncthreads();
+    }
+    const int lane = tid & 31, grp = lane >> 2, tig = lane & 3;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int ci = ci0 + j * 8 + tig * 2;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int co = co0 + warp * 16 + grp + half * 8;
+            if (co >= cout || ci >= cin) continue;
+            float *p = dw + ((int64_t)co * 27 + tap) * cin + ci;
+            atomicAdd(p, acc[j][half * 2]);
+            atomicAdd(p + 1, acc[j][half * 2 + 1]);
+        }
+    }
+}
+
+// wf[ci, tap, co] = w[co, 26 - tap, ci]: weights of the data-gradient convolution
+__global__ void k_flip_weights(const __nv_bfloat16 *__restrict__ w, int cout, int cin,
+                               __nv_bfloat16 *__restrict__ wf) {
+    const int64_t total = (int64_t)cout * 27 * cin;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ci = (int)(i % cin);
+        const int tap = (int)((i / cin) % 27);
+        const int co = (int)(i / ((int64_t)cin * 27));
+        wf[((int64_t)ci * 27 + (26 - tap)) * cout + co] = w[i];
+    }
+}
+
+// elementwise helpers over NDHWC slices
+__global__ void k_relu_bwd(__nv_bfloat16 *__restrict__ g, Act ga, const __nv_bfloat16 *__restrict__ y, Act ya,
+                           int c, int64_t nvox_total) {
+    const int64_t total = nvox_total * c;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = i / c;
+        const int ch = (int)(i - v * c);
+        if (!(__bfloat162float(y[v * ya.cstride + ya.coff + ch]) > 0.0f))
+            g[v * ga.cstride + ga.coff + ch] = __float2bfloat16(0.0f);
+    }
+}
+
+__global__ void k_bias_grad(const __nv_bfloat16 *__restrict__ g, Act ga, int c, int64_t nvox_total,
+                            float *__restrict__ db) {
+    // one block per channel group of 32; threads stride over voxels
+    const int ch = blockIdx.y * 32 + (threadIdx.x & 31);
+    float s = 0.0f;
+    if (ch < c)
+        for (int64_t v = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); v < nvox_total; v += (int64_t)gridDim.x * (blockDim.x / 32))
+            s += __bfloat162float(g[v * ga.cstride + ga.coff + ch]);
+    if (ch < c) atomicAdd(db + ch, s);
+}
+
+// 2x2x2 average pooling and its transpose; nearest 2x upsampling and its transpose
+__global__ void k_avgpool2(const __nv_bfloat16 *__restrict__ x, Act xa, __nv_bfloat16 *__restrict__ y, Act ya, int c) {
+    const int64_t total = (int64_t)ya.n * ya.d * ya.h * ya.w * c;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % c);
+        int64_t v = i / c;
+        const int ox = (int)(v % ya.w); v /= ya.w;
+        const int oy = (int)(v % ya.h); v /= ya.h;
+        const int oz = (int)(v % ya.d);
+        const int64_t nb = v / ya.d;
+        float s = 0.0f;
+        for (int k = 0; k < 8; ++k) {
+            const int zz = 2 * oz + (k >> 2), yy = 2 * oy + ((k >> 1) & 1), xx = 2 * ox + (k & 1);
+            if (zz < xa.d && yy < xa.h && xx < xa.w)
+                s += __bfloat162float(x[(((nb * xa.d + zz) * xa.h + yy) * xa.w + xx) * xa.cstride + xa.coff + ch]);
+        }
+        y[(((nb * ya.d + oz) * ya.h + oy) * ya.w + ox) * ya.cstride + ya.coff + ch] = __float2bfloat16(0.125f * s);
+    }
+}
+
+// dx (fine) = dy (coarse) / 8 for the 8 children (the adjoint of k_avgpool2)
+__global__ void k_avgpool2_bwd(const __nv_bfloat16 *__restrict__ dy, Act ya, __nv_bfloat16 *__restrict__ dx, Act xa, int c) {
+    const int64_t total = (int64_t)xa.n * xa.d * xa.h * xa.w * c;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % c);
+        int64_t v = i / c;
+        const int xx = (int)(v % xa.w); v /= xa.w;
+        const int yy = (int)(v % xa.h); v /= xa.h;
+        const int zz = (int)(v % xa.d);
+        const int64_t nb = v / xa.d;
+        const int oz = zz / 2, oy = yy / 2, ox = xx / 2;
+        float g = 0.0f;
+        if (oz < ya.d && oy < ya.h && ox < ya.w)
+            g = 0.125f * __bfloat162float(dy[(((nb * ya.d + oz) * ya.h + oy) * ya.w + ox) * ya.cstride + ya.coff + ch]);
+        dx[(((nb * xa.d + zz) * xa.h + yy) * xa.w + xx) * xa.cstride + xa.coff + ch] = __float2bfloat16(g);
+    }
+}
+
+// y (fine) = x (coarse) at the parent voxel; mode 1: the adjoint (sum of the 8 children)
+__global__ void k_upsample2(const __nv_bfloat16 *__restrict__ src, Act sa, __nv_bfloat16 *__restrict__ dst, Act da,
+                            int c, int adjoint) {
+    const int64_t total = (int64_t)da.n * da.d * da.h * da.w * c;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ch = (int)(i % c);
+        int64_t v = i / c;
+        const int ox = (int)(v % da.w); v /= da.w;
+        const int oy = (int)(v % da.h); v /= da.h;
+        const int oz = (int)(v % da.d);
+        const int64_t nb = v / da.d;
+        float r = 0.0f;
+        if (!adjoint) {  // dst fine, src coarse
+            r = __bfloat162float(src[(((nb * sa.d + oz / 2) * sa.h + oy / 2) * sa.w + ox / 2) * sa.cstride + sa.coff + ch]);
+        } else {  // dst coarse, src fine
+            for (int k = 0; k < 8; ++k) {
+                const int zz = 2 * oz + (k >> 2), yy = 2 * oy + ((k >> 1) & 1), xx = 2 * ox + (k & 1);
+                if (zz < sa.d && yy < sa.h && xx < sa.w)
+                    r += __bfloat162float(src[(((nb * sa.d + zz) * sa.h + yy) * sa.w + xx) * sa.cstride + sa.coff + ch]);
+            }
+        }
+        dst[(((nb * da.d + oz) * da.h + oy) * da.w + ox) * da.cstride + da.coff + ch] = __float2bfloat16(r);
+    }
+}
+
+// 1x1x1 head: out[v] = b + sum_c x[v, c] w[c] (FP32 out), and its gradients
+__global__ void k_head_fwd(const __nv_bfloat16 *__restrict__ x, Act xa, int c, const float *__restrict__ w,
+                           const float *__restrict__ bp, float *__restrict__ out, int64_t nvox_total) {
+    const float b = bp ? *bp : 0.0f;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nvox_total; v += (int64_t)gridDim.x * blockDim.x) {
+        float s = b;
+        for (int ch = 0; ch < c; ++ch) s = fmaf(__bfloat162float(x[v * xa.cstride + xa.coff + ch]), w[ch], s);
+        out[v] = s;
+    }
+}
+
+__global__ void k_head_bwd(const __nv_bfloat16 *__restrict__ x, Act xa, int c, const float *__restrict__ w,
+                           const float *__restrict__ gout, __nv_bfloat16 *__restrict__ gx, Act ga,
+                           float *__restrict__ gw, float *__restrict__ gb, int64_t nvox_total) {
+    __shared__ float sw[64];
+    __shared__ float sgw[64];
+    __shared__ float sgb;
+    for (int t = threadIdx.x; t < 64; t += blockDim.x) {
+        sw[t] = t < c ? w[t] : 0.0f;
+        sgw[t] = 0.0f;
+    }
+    if (threadIdx.x == 0) sgb = 0.0f;
+    __syncthreads();
+    float lgw[64];
+    for (int ch = 0; ch < 64; ++ch) lgw[ch] = 0.0f;
+    float lgb = 0.0f;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nvox_total; v += (int64_t)gridDim.x * blockDim.x) {
+        const float g = gout[v];
+        lgb += g;
+        for (int ch = 0; ch < c; ++ch) {
+            lgw[ch] = fmaf(g, __bfloat162float(x[v * xa.cstride + xa.coff + ch]), lgw[ch]);
+            gx[v * ga.cstride + ga.coff + ch] = __float2bfloat16(g * sw[ch]);
+        }
+    }
+    for (int ch = 0; ch < c; ++ch) atomicAdd(&sgw[ch], lgw[ch]);
+    atomicAdd(&sgb, lgb);
+    __syncthreads();
+    for (int t = threadIdx.x; t < c; t += blockDim.x) atomicAdd(gw + t, sgw[t]);
+    if (threadIdx.x == 0) atomicAdd(gb, sgb);
+}
+
+// Adam on FP32 masters, refreshed BF16 copy (bf may be NULL for FP32-only parameters)
+__global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__restrict__ v,
+                       const float *__restrict__ g, __nv_bfloat16 *__restrict__ bf, int64_t n,
+                       float lr, float b1, float b2, float eps, float c1, float c2) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        w[i] = wi;
+        if (bf) bf[i] = __float2bfloat16(wi);
+    }
+}
+
+// dst slice += src slice (gradients of a tensor used twice, e.g. a U-Net skip)
+__global__ void k_add(__nv_bfloat16 *__restrict__ dst, Act da, const __nv_bfloat16 *__restrict__ src, Act sa,
+                      int c, int64_t nvox_total) {
+    const int64_t total = nvox_total * c;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = i / c;
+        const int ch = (int)(i - v * c);
+        __nv_bfloat16 *d = dst + v * da.cstride + da.coff + ch;
+        *d = __float2bfloat16(__bfloat162float(*d) + __bfloat162float(src[v * sa.cstride + sa.coff + ch]));
+    }
+}
+
+// relative squared error per sample: loss += sum m (p - t)^2 * inv_den[s]; grad = 2 m (p - t) inv_den[s] / n_samples
+__global__ void k_rel_mse(const float *__restrict__ pred, const float *__restrict__ target,
+                          const float *__restrict__ mask, const float *__restrict__ inv_den, int64_t per_sample,
+                          int n_samples, float *__restrict__ grad, double *__restrict__ loss) {
+    double acc = 0.0;
+    const int64_t total = per_sample * n_samples;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(i / per_sample);
+        const float m = mask ? mask[i - (int64_t)s * per_sample] : 1.0f;
+        const float d = pred[i] - target[i];
+        acc += (double)(m * d * d) * (double)inv_den[s] / (double)n_samples;
+        if (grad) grad[i] = 2.0f * m * d * inv_den[s] / (float)n_samples;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(loss, acc);
+}
+
+// trilinear 2x upsampling of a single-channel FP32 volume (cell-centred samples)
+__global__ void k_trilinear2(const float *__restrict__ src, int n, int d, int h, int w, float *__restrict__ dst,
+                             int D, int H, int W) {
+    const int64_t total = (int64_t)n * D * H * W;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t v = i;
+        const int ox = (int)(v % W); v /= W;
+        const int oy = (int)(v % H); v /= H;
+        const int oz = (int)(v % D);
+        const int64_t nb = v / D;
+        const float fz = fminf(fmaxf((oz + 0.5f) * 0.5f - 0.5f, 0.0f), (float)(d - 1));
+        const float fy = fminf(fmaxf((oy + 0.5f) * 0.5f - 0.5f, 0.0f), (float)(h - 1));
+        const float fx = fminf(fmaxf((ox + 0.5f) * 0.5f - 0.5f, 0.0f), (float)(w - 1));
+        const int z0 = (int)fz, y0 = (int)fy, x0 = (int)fx;
+        const int z1 = min(z0 + 1, d - 1), y1 = min(y0 + 1, h - 1), x1 = min(x0 + 1, w - 1);
+        const float az = fz - z0, ay = fy - y0, ax = fx - x0;
+        const float *b = src + nb * (int64_t)d * h * w;
+        auto at = [&](int z, int y, int x) { return b[((int64_t)z * h + y) * w + x]; };
+        const float c00 = at(z0, y0, x0) * (1 - ax) + at(z0, y0, x1) * ax;
+        const float c01 = at(z0, y1, x0) * (1 - ax) + at(z0, y1, x1) * ax;
+        const float c10 = at(z1, y0, x0) * (1 - ax) + at(z1, y0, x1) * ax;
+        const float c11 = at(z1, y1, x0) * (1 - ax) + at(z1, y1, x1) * ax;
+        dst[i] = ((c00 * (1 - ay) + c01 * ay) * (1 - az) + (c10 * (1 - ay) + c11 * ay) * az);
+    }
+}
+
+inline int check_act(const Act &a, int c, const char *name) {
+    if (a.n <= 0 || a.d <= 0 || a.h <= 0 || a.w <= 0) return fail(SRF_EGRID, "%s: bad shape", name);
+    if (a.cstride < c + a.coff || a.coff < 0) return fail(SRF_EGRID, "%s: channel slice exceeds stride", name);
+    if ((int64_t)a.n * a.d * a.h * a.w * a.cstride >= (int64_t(1) << 40)) return fail(SRF_ERANGE, "%s: too large", name);
+    return SRF_OK;
+}
+
+inline Act act_of(const int32_t s[6]) { return Act{s[0], s[1], s[2], s[3], s[4], s[5]}; }
+
+}  // namespace srf
+
+using namespace srf;
+
+extern "C" {
+
+int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *w, const float *bias,
+                   int32_t cout, int32_t relu, void *y, const int32_t ys[6], float *yf, void *stream) {
+    if (!x || !xs || !w || !y || !ys) return fail(SRF_EINVAL, "NULL argument");
+    const Act xa = act_of(xs), ya = act_of(ys);
+    int rc;
+    if ((rc = check_act(xa, cin, "x")) || (rc = check_act(ya, cout, "y"))) return rc;
+    if (cin % 16 || cout % 16 || xa.cstride % 8 || xa.coff % 8 || ya.cstride % 2 || ya.coff % 2)
+        return fail(SRF_EINVAL, "conv3d needs Cin, Cout multiples of 16 and 16-byte aligned channel slices");
+    if (xa.n != ya.n || xa.d != ya.d || xa.h != ya.h || xa.w != ya.w) return fail(SRF_EGRID, "x/y shapes differ");
+    const int64_t nvox = (int64_t)xa.d * xa.h * xa.w;
+    dim3 grid((unsigned)((nvox + kCM - 1) / kCM), (unsigned)((cout + kCN - 1) / kCN), (unsigned)xa.n);
+    k_conv3d_fwd<<<grid, 128, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)x, xa, cin, (const __nv_bfloat16 *)w,
+                                                        bias, cout, relu, (__nv_bfloat16 *)y, ya, yf);
+    return check_cuda("conv3d forward launch");
+}
+
+int srf_conv3d_wgrad(const void *x, const int32_t xs[6], int32_t cin, const void *dy, const int32_t ds[6],
+                     int32_t cout, float *dw, void *stream) {
+    if (!x || !xs || !dy || !ds || !dw) return fail(SRF_EINVAL, "NULL argument");
+    const Act xa = act_of(xs), da = act_of(ds);
+    int rc;
+    if ((rc = check_act(xa, cin, "x")) || (rc = check_act(da, cout, "dy"))) return rc;
+    if (cin % 16 || cout % 16 || xa.cstride % 8 || xa.coff % 8 || da.cstride % 8 || da.coff % 8)
+        return fail(SRF_EINVAL, "conv3d needs Cin, Cout multiples of 16 and 16-byte aligned channel slices");
+    const int64_t total = (int64_t)xa.n * xa.d * xa.h * xa.w;
+    const int tiles = ((cout + kCM - 1) / kCM) * ((cin + kCN - 1) / kCN);
+    // enough splits to fill the GPU: ~4 CTAs per SM over 27 taps x tiles
+    int64_t want = (int64_t)num_sms() * 8 / (27 * tiles) + 1;
+    int64_t per = (total + want - 1) / want;
+    per = ((per + kCK - 1) / kCK) * kCK;
+    const int64_t splits = (total + per - 1) / per;
+    dim3 grid((unsigned)splits, 27, (unsigned)tiles);
+    k_conv3d_wgrad<<<grid, 128, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)x, xa, cin, (const __nv_bfloat16 *)dy,
+                                                          da, cout, dw, per);
+    return check_cuda("conv3d weight-gradient launch");
+}
+
+int srf_conv3d_flip_weights(const void *w, int32_t cout, int32_t cin, void *wf, void *stream) {
+    if (!w || !wf || cout <= 0 || cin <= 0) return fail(SRF_EINVAL, "bad arguments");
+    const int64_t total = (int64_t)cout * 27 * cin;
+    k_flip_weights<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        (const __nv_bfloat16 *)w, cout, cin, (__nv_bfloat16 *)wf);
+    return check_cuda("flip weights launch");
+}
+
+int srf_cnn_relu_bwd(void *g, const int32_t gs[6], const void *y, const int32_t ys[6], int32_t c, void *stream) {
+    const Act ga = act_of(gs), ya = act_of(ys);
+    int rc;
+    if ((rc = check_act(ga, c, "g")) || (rc = check_act(ya, c, "y"))) return rc;
+    const int64_t nv = (int64_t)ga.n * ga.d * ga.h * ga.w;
+    unsigned blocks = grid_for(k_relu_bwd, nv * c, 256);
+    k_relu_bwd<<<blocks, 256, 0, (cudaStream_t)stream>>>((__nv_bfloat16 *)g, ga, (const __nv_bfloat16 *)y, ya, c, nv);
+    return check_cuda("relu backward launch");
+}
+
+int srf_cnn_bias_grad(const void *g, const int32_t gs[6], int32_t c, float *db, void *stream) {
+    const Act ga = act_of(gs);
+    int rc;
+    if ((rc = check_act(ga, c, "g"))) return rc;
+    const int64_t nv = (int64_t)ga.n * ga.d * ga.h * ga.w;
+    dim3 grid((unsigned)std::min<int64_t>(1024, (nv + 7) / 8), (unsigned)((c + 31) / 32));
+    k_bias_grad<<<grid, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)g, ga, c, nv, db);
+    return check_cuda("bias gradient launch");
+}
+
+int srf_cnn_pool2(const void *x, const int32_t xs[6], void *y, const int32_t ys[6], int32_t c, int32_t adjoint,
+                  void *stream) {
+    const Act xa = act_of(xs), ya = act_of(ys);  // x fine, y coarse
+    int rc;
+    if ((rc = check_act(xa, c, "fine")) || (rc = check_act(ya, c, "coarse"))) return rc;
+    if (ya.d != (xa.d + 1) / 2 || ya.h != (xa.h + 1) / 2 || ya.w != (xa.w + 1) / 2 || xa.n != ya.n)
+        return fail(SRF_EGRID, "coarse grid must be ceil(fine / 2)");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!adjoint) {
+        const int64_t t = (int64_t)ya.n * ya.d * ya.h * ya.w * c;
+        k_avgpool2<<<grid_for(k_avgpool2, t, 256), 256, 0, s>>>((const __nv_bfloat16 *)x, xa, (__nv_bfloat16 *)y, ya, c);
+    } else {  // y holds the coarse gradient, x receives the fine gradient
+        const int64_t t = (int64_t)xa.n * xa.d * xa.h * xa.w * c;
+        k_avgpool2_bwd<<<grid_for(k_avgpool2_bwd, t, 256), 256, 0, s>>>((const __nv_bfloat16 *)y, ya, (__nv_bfloat16 *)x, xa, c);
+    }
+    return check_cuda("pool launch");
+}
+
+int srf_cnn_upsample2(const void *coarse, const int32_t cs[6], void *fine, const int32_t fs[6], int32_t c,
+                      int32_t adjoint, void *stream) {
+    const Act ca = act_of(cs), fa = act_of(fs);
+    int rc;
+    if ((rc = check_act(ca, c, "coarse")) || (rc = check_act(fa, c, "fine"))) return rc;
+    if (ca.d != (fa.d + 1) / 2 || ca.h != (fa.h + 1) / 2 || ca.w != (fa.w + 1) / 2 || ca.n != fa.n)
+        return fail(SRF_EGRID, "coarse grid must be ceil(fine / 2)");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!adjoint) {
+        const int64_t t = (int64_t)fa.n * fa.d * fa.h * fa.w * c;
+        k_upsample2<<<grid_for(k_upsample2, t, 256), 256, 0, s>>>((const __nv_bfloat16 *)coarse, ca, (__nv_bfloat16 *)fine, fa, c, 0);
+    } else {  // fine holds the gradient, coarse receives the sum over children
+        const int64_t t = (int64_t)ca.n * ca.d * ca.h * ca.w * c;
+        k_upsample2<<<grid_for(k_upsample2, t, 256), 256, 0, s>>>((const __nv_bfloat16 *)fine, fa, (__nv_bfloat16 *)coarse, ca, c, 1);
+    }
+    return check_cuda("upsample launch");
+}
+
+int srf_cnn_head(const void *x, const int32_t xs[6], int32_t c, const float *w, const float *b, float *out,
+                 const float *gout, void *gx, const int32_t gs[6], float *gw, float *gb, void *stream) {
+    if (c <= 0 || c > 64) return fail(SRF_EINVAL, "head supports 1..64 channels");
+    const Act xa = act_of(xs);
+    int rc;
+    if ((rc = check_act(xa, c, "x"))) return rc;
+    const int64_t nv = (int64_t)xa.n * xa.d * xa.h * xa.w;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!gout) {
+        k_head_fwd<<<grid_for(k_head_fwd, nv, 256), 256, 0, s>>>((const __nv_bfloat16 *)x, xa, c, w, b, out, nv);
+    } else {
+        const Act ga = act_of(gs);
+        if ((rc = check_act(ga, c, "gx"))) return rc;
+        unsigned blocks = (unsigned)std::min<int64_t>((nv + 255) / 256, (int64_t)num_sms() * 4);
+        k_head_bwd<<<blocks, 256, 0, s>>>((const __nv_bfloat16 *)x, xa, c, w, gout, (__nv_bfloat16 *)gx, ga, gw, gb, nv);
+    }
+    return check_cuda("head launch");
+}
+
+int srf_cnn_add(void *dst, const int32_t ds[6], const void *src, const int32_t ss[6], int32_t c, void *stream) {
+    const Act da = act_of(ds), sa = act_of(ss);
+    int rc;
+    if ((rc = check_act(da, c, "dst")) || (rc = check_act(sa, c, "src"))) return rc;
+    const int64_t nv = (int64_t)da.n * da.d * da.h * da.w;
+    k_add<<<grid_for(k_add, nv * c, 256), 256, 0, (cudaStream_t)stream>>>((__nv_bfloat16 *)dst, da,
+                                                                         (const __nv_bfloat16 *)src, sa, c, nv);
+    return check_cuda("add launch");
+}
+
+int srf_cnn_rel_mse(const float *pred, const float *target, const float *mask, const float *inv_den,
+                    int64_t per_sample, int32_t n_samples, float *grad, double *loss, void *stream) {
+    if (!pred || !target || !inv_den || !loss || per_sample <= 0 || n_samples <= 0) return fail(SRF_EINVAL, "bad arguments");
+    k_rel_mse<<<grid_for(k_rel_mse, per_sample * n_samples, 256), 256, 0, (cudaStream_t)stream>>>(
+        pred, target, mask, inv_den, per_sample, n_samples, grad, loss);
+    return check_cuda("loss launch");
+}
+
+int srf_cnn_trilinear2(const float *src, int32_t n, int32_t d, int32_t h, int32_t w, float *dst, int32_t D,
+                       int32_t H, int32_t W, void *stream) {
+    if (!src || !dst || n <= 0 || d <= 0 || h <= 0 || w <= 0 || D <= 0 || H <= 0 || W <= 0) return fail(SRF_EINVAL, "bad arguments");
+    const int64_t t = (int64_t)n * D * H * W;
+    k_trilinear2<<<grid_for(k_trilinear2, t, 256), 256, 0, (cudaStream_t)stream>>>(src, n, d, h, w, dst, D, H, W);
+    return check_cuda("trilinear launch");
+}
+
+int srf_cnn_adam(float *w, float *m, float *v, const float *g, void *bf16_copy, int64_t n, float lr,
+                 float b1, float b2, float eps, int32_t step, void *stream) {
+    if (!w || !m || !v || !g || n < 0 || step < 1) return fail(SRF_EINVAL, "bad arguments");
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    k_adam<<<grid_for(k_adam, n, 256), 256, 0, (cudaStream_t)stream>>>(w, m, v, g, (__nv_bfloat16 *)bf16_copy, n,
+                                                                       lr, b1, b2, eps, c1, c2);
+    return check_cuda("adam launch");
+}
+
+}  // extern "C"

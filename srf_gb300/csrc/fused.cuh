@@ -25,7 +25,7 @@ struct __align__(16) LorRec {
     float kq, kz, wc, invL2;
     float ratio1, L, yv, pd;
     float inv_pd, Aq, Bq, Az;  // fast forms: boundary(pp) ~= fmaf(B, pp, A)
-    float Bz, mq, mz, pad0;    // mq, mz: floor margins of the fast forms
+    float Bz, mq, mz, ad;      // mq, mz: floor margins of the fast forms; ad: additive term
     int lo, hi, flags, pad1;
 };
 constexpr int F_VALID = 1, F_PROJ = 2, F_XDOM = 4, F_TIE = 8;
@@ -152,7 +152,6 @@ __device__ __forceinline__ LorRec setup_rec(const float *l, float tv, float yv, 
     const float e = 9.5367431640625e-7f;  // 2^-20
     R.mq = e * ((fabsf(R.kq) * (fabsf(R.p1) + (float)np) + fabsf(R.q1)) / dq + nq2 + 2.0f);
     R.mz = e * ((fabsf(R.kz) * (fabsf(R.p1) + (float)np) + fabsf(z1)) / k.dz + k.nz2 + 2.0f);
-    R.pad0 = 0.0f;
     R.pad1 = 0;
     return R;
 }

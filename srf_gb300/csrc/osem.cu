@@ -15,7 +15,7 @@ namespace srf {
 // Generic path for a LOR whose projector and backprojector traverse along different axes
 // (non-TOF with |xd| == |yd|): two setups, as in the standalone kernels.
 template <int G, bool TOF>
-__device__ __forceinline__ void tie_path(const float *l, float tv, float yv, int lane, const Grid &g,
+__device__ __forceinline__ void tie_path(const float *l, float tv, float yv, float ad, int lane, const Grid &g,
                                          const TofParams &tp, const View &x, const View &xt,
                                          const View &bp, const View &bpt, int rule, float eps,
                                          double &ll, bool want_ll) {
@@ -27,7 +27,7 @@ __device__ __forceinline__ void tie_path(const float *l, float tv, float yv, int
             slab<TOF, RULES_PROJ>(S, ip, [&](int32_t off, float w) { acc += __ldg(im + off) * w; });
     }
     const float p = group_sum<G>(acc);
-    const float den = __fadd_rn(p, eps);
+    const float den = __fadd_rn(__fadd_rn(p, ad), eps);
     const float r = (rule == SRF_RATIO_DIV_NO_NAN) ? ((den == 0.0f) ? 0.0f : __fdiv_rn(yv, den)) : __fdiv_rn(yv, den);
     if (want_ll && lane == 0 && den > 0.0f) ll += (double)yv * (double)__logf(den);
     if (r != 0.0f && setup_lor<TOF, RULES_BACK>(l[0], l[1], l[2], l[3], l[4], l[5], tv, g, tp, bp.st, bpt.st, bpt.ptr != nullptr, S)) {
@@ -70,7 +70,8 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
                                                 int64_t n, int stride, const float *__restrict__ tof,
                                                 int tof_stride, const Grid &g, const GridK &k,
                                                 const TofParams &tp, const float *__restrict__ y,
-                                                int rule, float eps, const View &x, const View &xt,
+                                                const float *__restrict__ add, int rule, float eps,
+                                                const View &x, const View &xt,
                                                 const View &bp, const View &bpt, int64_t base,
                                                 bool want_ll, double &ll) {
     constexpr int GPW = 32 / G;
@@ -90,6 +91,7 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
             const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
             const float yv = y ? __ldg(y + i) : 1.0f;
             R = setup_rec<TOF>(lv, tv, yv, g, k);
+            R.ad = add ? __ldg(add + i) : 0.0f;
         }
         store_rec(&wrecs[lane32], R);
     }
@@ -104,7 +106,7 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
 #pragma unroll
             for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
             const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
-            tie_path<G, TOF>(lv, tv, R.yv, lane, g, tp, x, xt, bp, bpt, rule, eps, ll, want_ll);
+            tie_path<G, TOF>(lv, tv, R.yv, R.ad, lane, g, tp, x, xt, bp, bpt, rule, eps, ll, want_ll);
             continue;
         }
         const bool valid = R.flags & F_VALID;
@@ -136,7 +138,7 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
         }
         const float p = group_sum<G>(acc) * R.invL2;
         if (!valid) continue;
-        const float den = __fadd_rn(p, eps);
+        const float den = __fadd_rn(__fadd_rn(p, R.ad), eps);
         float r;
         if (rule == SRF_RATIO_DIV_NO_NAN)
             r = (den == 0.0f) ? 0.0f : __fdiv_rn(R.yv, den);
@@ -170,8 +172,9 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
 template <int G, bool TOF, int U, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB)
 k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
-              int tof_stride, Grid g, TofParams tp, const float *__restrict__ y, int rule, float eps,
-              View x, View xt, View bp, View bpt, double *__restrict__ loglik) {
+              int tof_stride, Grid g, TofParams tp, const float *__restrict__ y,
+              const float *__restrict__ add, int rule, float eps, View x, View xt, View bp, View bpt,
+              double *__restrict__ loglik) {
     __shared__ LorRec recs[kBlock / 32][32];
     const int wib = threadIdx.x >> 5;
     const int lane32 = threadIdx.x & 31;
@@ -181,7 +184,7 @@ k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float
     const bool want_ll = loglik != nullptr;
     double ll = 0.0;
     for (int64_t base = warp * 32; base < n; base += nwarps * 32) {
-        osem_warp_batch<G, TOF, U>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, y, rule, eps, x, xt, bp, bpt, base, want_ll, ll);
+        osem_warp_batch<G, TOF, U>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, y, add, rule, eps, x, xt, bp, bpt, base, want_ll, ll);
     }
     if (want_ll) {
 #pragma unroll
@@ -192,34 +195,34 @@ k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float
 
 template <int G, bool TOF, int U, int MINB>
 static int launch_osem_g(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
-                         const Grid &g, const TofParams &tp, const float *y, int rule, float eps,
+                         const Grid &g, const TofParams &tp, const float *y, const float *add, int rule, float eps,
                          const View &x, const View &xt, const View &bp, const View &bpt,
                          double *loglik, cudaStream_t s) {
     auto kern = k_osem_subset<G, TOF, U, MINB>;
     unsigned blocks = grid_for(kern, n, kBlock);
-    kern<<<blocks, kBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik);
+    kern<<<blocks, kBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik);
     return check_cuda("osem subset kernel launch");
 }
 
 template <int G, bool TOF>
 static int launch_osem_u(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
-                         const Grid &g, const TofParams &tp, const float *y, int rule, float eps,
+                         const Grid &g, const TofParams &tp, const float *y, const float *add, int rule, float eps,
                          const View &x, const View &xt, const View &bp, const View &bpt,
                          double *loglik, cudaStream_t s) {
     if (slabs_per_lane() == 2)
-        return launch_osem_g<G, TOF, 2, 3>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
-    return launch_osem_g<G, TOF, 4, 2>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
+        return launch_osem_g<G, TOF, 2, 3>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik, s);
+    return launch_osem_g<G, TOF, 4, 2>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik, s);
 }
 
 template <bool TOF>
 static int launch_osem(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
-                       const Grid &g, const TofParams &tp, const float *y, int rule, float eps,
+                       const Grid &g, const TofParams &tp, const float *y, const float *add, int rule, float eps,
                        const View &x, const View &xt, const View &bp, const View &bpt,
                        double *loglik, cudaStream_t s) {
     switch (group_lanes()) {
-    case 8: return launch_osem_u<8, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
-    case 16: return launch_osem_u<16, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
-    default: return launch_osem_u<32, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, rule, eps, x, xt, bp, bpt, loglik, s);
+    case 8: return launch_osem_u<8, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik, s);
+    case 16: return launch_osem_u<16, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik, s);
+    default: return launch_osem_u<32, TOF>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik, s);
     }
 }
 
@@ -317,33 +320,76 @@ __device__ __forceinline__ bool study_ok(const srf_study &st) {
            ((st.x_t == nullptr) == (st.bp_t == nullptr));
 }
 
+constexpr int kMaxStudiesSmem = 1024;
+
+// One warp's current study, decoded once when the warp enters it and read through shared memory:
+// in registers the grid constants and the four image views would push the traversal past its
+// register budget (the single-study kernel gets them from the parameter bank instead).
+struct WarpStudy {
+    const float *lors, *tof, *y;
+    int64_t n;
+    int stride, tof_stride, ok;
+    Grid g;
+    GridK k;
+    View x, xt, bp, bpt;
+};
+
+template <bool TOF>
+__device__ __forceinline__ void decode_study(const srf_study &st, const TofParams &tp, WarpStudy &w) {
+    w.ok = study_ok(st) && !(TOF && (st.tof == nullptr || st.tof_stride < 1));
+    if (!w.ok) return;
+    w.lors = st.lors; w.tof = st.tof; w.y = st.y;
+    w.n = st.n; w.stride = st.lor_stride; w.tof_stride = st.tof_stride;
+    w.g = Grid{st.grid[0], st.grid[1], st.grid[2], st.center[0], st.center[1], st.center[2],
+               st.size[0], st.size[1], st.size[2]};
+    w.k = make_gridk<TOF>(w.g, tp);
+    const int64_t nxy = (int64_t)w.g.nx * w.g.ny;
+    w.x = View{st.x, {1, w.g.nx, nxy}};
+    w.bp = View{st.bp, {1, w.g.nx, nxy}};
+    w.xt = View{st.x_t, {w.g.ny, 1, nxy}};
+    w.bpt = View{st.bp_t, {w.g.ny, 1, nxy}};
+}
+
 // Persistent kernel over all studies' LOR batches: warp-batch b belongs to the study s with
-// boff[s] <= b < boff[s + 1] (32 LORs per batch, each study padded to whole batches).
+// boff[s] <= b < boff[s + 1] (32 LORs per batch, each study padded to whole batches). The batch
+// offsets are staged in shared memory (when they fit), so the lookup costs a few shared-memory
+// reads per batch, and a warp decodes a study descriptor only when it moves to another study.
 template <int G, bool TOF, int U, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB)
 k_osem_batch(const srf_study *__restrict__ studies, int n_studies, const int64_t *__restrict__ boff,
              int64_t total_batches, TofParams tp, int rule, float eps, double *__restrict__ loglik) {
     __shared__ LorRec recs[kBlock / 32][32];
+    __shared__ int64_t soff[kMaxStudiesSmem + 1];
+    __shared__ WarpStudy wst[kBlock / 32];
+    const bool staged = n_studies <= kMaxStudiesSmem;
+    if (staged)
+        for (int t = threadIdx.x; t <= n_studies; t += blockDim.x) soff[t] = __ldg(boff + t);
+    __syncthreads();
+    const int64_t *off = staged ? soff : boff;
     const int wib = threadIdx.x >> 5;
     const int lane32 = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const bool want_ll = loglik != nullptr;
+    WarpStudy &w = wst[wib];
     double ll = 0.0;
+    int s = -1;
     for (int64_t b = warp; b < total_batches; b += nwarps) {
-        const int s = find_segment(boff, n_studies, b);
-        const srf_study st = studies[s];
-        if (!study_ok(st)) continue;  // uniform over the warp
-        if (TOF && (st.tof == nullptr || st.tof_stride < 1)) continue;
-        const Grid g{st.grid[0], st.grid[1], st.grid[2], st.center[0], st.center[1], st.center[2],
-                     st.size[0], st.size[1], st.size[2]};
-        const GridK k = make_gridk<TOF>(g, tp);
-        const int64_t nxy = (int64_t)g.nx * g.ny;
-        const View x{st.x, {1, g.nx, nxy}}, bp{st.bp, {1, g.nx, nxy}};
-        const View xt{st.x_t, {g.ny, 1, nxy}}, bpt{st.bp_t, {g.ny, 1, nxy}};
-        const int64_t base = (b - __ldg(boff + s)) * 32;
-        osem_warp_batch<G, TOF, U>(recs[wib], st.lors, st.n, st.lor_stride, st.tof, st.tof_stride,
-                                   g, k, tp, st.y, rule, eps, x, xt, bp, bpt, base, want_ll, ll);
+        if (s < 0 || b < off[s] || b >= off[s + 1]) {  // uniform over the warp
+            int lo = 0, hi = n_studies;  // off[lo] <= b < off[hi]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (off[mid] <= b) lo = mid; else hi = mid;
+            }
+            s = lo;
+            __syncwarp();
+            if (lane32 == 0) decode_study<TOF>(studies[s], tp, w);
+            __syncwarp();
+        }
+        if (!w.ok) continue;
+        osem_warp_batch<G, TOF, U>(recs[wib], w.lors, w.n, w.stride, w.tof, w.tof_stride, w.g, w.k, tp,
+                                   w.y, nullptr, rule, eps, w.x, w.xt, w.bp, w.bpt,
+                                   (b - off[s]) * 32, want_ll, ll);
     }
     if (want_ll) {
 #pragma unroll
@@ -436,7 +482,7 @@ int srf_osem_update_batch(const srf_study *studies, int32_t n_studies, const int
 
 int srf_osem_subset(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
                     int32_t tof_stride, float tof_bin, float tof_sigma2, float tof_nsigma,
-                    const float *y, int32_t ratio_rule, float eps, const float *x,
+                    const float *y, const float *add, int32_t ratio_rule, float eps, const float *x,
                     const float *x_t, float *bp, float *bp_t, const int32_t grid[3],
                     const float center[3], const float size[3], double *loglik, void *stream) {
     Grid g; int rc;
@@ -458,10 +504,10 @@ int srf_osem_subset(const float *lors, int64_t n, int32_t lor_stride, const floa
     if (tof) {
         TofParams tp;
         if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
-        return launch_osem<true>(lors, n, lor_stride, tof, tof_stride, g, tp, y, ratio_rule, eps, vx, vxt, vbp, vbpt, loglik, s);
+        return launch_osem<true>(lors, n, lor_stride, tof, tof_stride, g, tp, y, add, ratio_rule, eps, vx, vxt, vbp, vbpt, loglik, s);
     }
     TofParams tp{0, 0, 0};
-    return launch_osem<false>(lors, n, lor_stride, nullptr, 1, g, tp, y, ratio_rule, eps, vx, vxt, vbp, vbpt, loglik, s);
+    return launch_osem<false>(lors, n, lor_stride, nullptr, 1, g, tp, y, add, ratio_rule, eps, vx, vxt, vbp, vbpt, loglik, s);
 }
 
 int srf_osem_update(float *x, float *x_t, float *bp, float *bp_t, const float *emap,

@@ -162,14 +162,14 @@ class SubsetState:
 
     def subset(self, lors: torch.Tensor, y: Optional[torch.Tensor], *, rule: int, eps: float,
                tof: Optional[Tuple[float, float]] = None, tof_nsigma: float = 0.0,
-               track_loglik: bool = False) -> None:
+               track_loglik: bool = False, add: Optional[torch.Tensor] = None) -> None:
         n, stride = check_lors(lors, tof is not None)
         if y is not None:
             _require_cuda(y, "y")
         tof_p = _tof_ptr(lors) if tof is not None else None
         tb, ts = tof if tof is not None else (0.0, 0.0)
         call("srf_osem_subset", ptr(lors), i64(n), i32(stride), tof_p, i32(stride),
-             *_tof_args(tb, ts, tof_nsigma), ptr(y), i32(rule), f32(eps), ptr(self.x),
+             *_tof_args(tb, ts, tof_nsigma), ptr(y), ptr(add), i32(rule), f32(eps), ptr(self.x),
              ptr(self.x_t), ptr(self.bp), ptr(self.bp_t), i32x3(self.shape),
              f32x3(self.center), f32x3(self.size), ptr(self.loglik) if track_loglik else None,
              stream_ptr(lors.device))

@@ -194,6 +194,7 @@ class OsemFullTof(_NefLike):
     emap_scale: Optional[float] = None   # default 1 / n_sub
     seed: int = 0
     snap: bool = False
+    add: Any = None                      # per-event additive expected counts (e.g. scatter)
 
     def prepare(self):
         """Device-resident inputs: LORs and values permuted into subset order once."""
@@ -205,6 +206,9 @@ class OsemFullTof(_NefLike):
         perm = torch.as_tensor(np.random.default_rng(self.seed).permutation(n), device=dev)
         lors = lors.index_select(0, perm).contiguous()
         y = y.index_select(0, perm).contiguous()
+        # a frozen record: the permuted additive term is cached beside the fields
+        object.__setattr__(self, "_add", None if self.add is None
+                           else to_dev(self.add).index_select(0, perm).contiguous())
         scale = (1.0 / self.n_sub) if self.emap_scale is None else self.emap_scale
         em = (_emap_dev(self.emap) * scale)
         return lors, y, em
@@ -217,11 +221,13 @@ class OsemFullTof(_NefLike):
         n = lors.shape[0]
         n_per = n // self.n_sub
         tof = (self.scanner.tof.tof_bin, self.scanner.tof.tof_sigma2)
+        add = getattr(self, "_add", None)
         for _ in range(self.n_iter if n_iter is None else n_iter):
             for k in range(self.n_sub):
                 sl = slice(k * n_per, (k + 1) * n_per)
                 st.subset(lors[sl], None if y is None else y[sl], rule=SRF_RATIO_DIV_NO_NAN,
-                          eps=1e-5, tof=tof, tof_nsigma=self.tof_nsigma, track_loglik=track_loglik)
+                          eps=1e-5, tof=tof, tof_nsigma=self.tof_nsigma, track_loglik=track_loglik,
+                          add=None if add is None else add[sl])
                 st.update(em, guard_zero=True)
         return st
 

@@ -1,0 +1,432 @@
+"""Learned single-scatter surrogate (not in the reference).
+
+A 3-D U-Net of about 1.1M parameters maps sinogram-domain features of a study (emission line
+integrals and attenuation factors along each bin's LOR) to the single-scatter-simulation
+sinogram. Every layer runs on hand-written kernels (srf_gb300/csrc/cnn.cu): BF16 activations
+and weights, FP32 accumulation on the tensor cores for the 3x3x3 convolutions (forward, data
+gradient through flipped weights, split-K weight gradient), FP32 master weights under Adam.
+
+Architecture on a (D, H, W) grid (the half-resolution sinogram), channels (32, 64, 96):
+    e1a, e1b: 3x3x3 16->32->32            (input: 2 feature channels padded to 16)
+    pool -> e2a, e2b: 32->64->64
+    pool -> e3a, e3b: 64->96->96
+    up + skip(e2b) -> d2a, d2b: 160->64->64
+    up + skip(e1b) -> d1a, d1b: 96->32->32
+    1x1x1 head: 32->1 (FP32)
+ReLU after every 3x3x3 convolution. Skip concatenation is free: e1b/e2b write straight into the
+channel slices the decoder reads.
+
+``ScatterSurrogate`` wraps the network with SSS as the judge: ``estimate`` predicts the scatter
+sinogram and, when a spot-check SSS on a subset of bins differs by more than ``fallback_tol``
+relative L2, returns the full SSS instead.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import Dict, List, Optional, Tuple
+
+import torch
+
+from ._lib import call, f32, i32, i64, ptr, stream_ptr
+
+BF16 = torch.bfloat16
+F32 = torch.float32
+
+
+def act(t: torch.Tensor, coff: int = 0):
+    """int32[6] NDHWC descriptor of a (N, D, H, W, C) tensor (a channel slice from coff)."""
+    n, d, h, w, c = t.shape
+    return (ctypes.c_int32 * 6)(n, d, h, w, c, coff)
+
+
+def half(shape):
+    return tuple((s + 1) // 2 for s in shape)
+
+
+class Conv3:
+    """3x3x3 convolution parameters: FP32 master weights [Cout][27][Cin], BF16 copies."""
+
+    def __init__(self, cin: int, cout: int, gen: torch.Generator, device):
+        std = math.sqrt(2.0 / (27 * cin))
+        self.cin, self.cout = cin, cout
+        self.w = (torch.randn(cout, 27, cin, generator=gen) * std).to(device)
+        self.b = torch.zeros(cout, device=device)
+        self.gw = torch.zeros_like(self.w)
+        self.gb = torch.zeros_like(self.b)
+        self.wb = self.w.to(BF16)
+        self.wf = torch.empty(cin, 27, cout, dtype=BF16, device=device)
+
+    def params(self):
+        return [(self.w, self.gw, self.wb), (self.b, self.gb, None)]
+
+    def refresh(self, stream):
+        call("srf_conv3d_flip_weights", ptr(self.wb), i32(self.cout), i32(self.cin), ptr(self.wf), stream)
+
+
+class UNet3D:
+    IN_CH = 16
+
+    def __init__(self, channels=(32, 64, 96), seed: int = 0, device="cuda"):
+        g = torch.Generator().manual_seed(seed)
+        self.device = torch.device(device)
+        c1, c2, c3 = channels
+        self.c = channels
+        self.e1a, self.e1b = Conv3(self.IN_CH, c1, g, self.device), Conv3(c1, c1, g, self.device)
+        self.e2a, self.e2b = Conv3(c1, c2, g, self.device), Conv3(c2, c2, g, self.device)
+        self.e3a, self.e3b = Conv3(c2, c3, g, self.device), Conv3(c3, c3, g, self.device)
+        self.d2a, self.d2b = Conv3(c3 + c2, c2, g, self.device), Conv3(c2, c2, g, self.device)
+        self.d1a, self.d1b = Conv3(c2 + c1, c1, g, self.device), Conv3(c1, c1, g, self.device)
+        self.hw = (torch.randn(c1, generator=g) * math.sqrt(1.0 / c1)).to(self.device)
+        self.hb = torch.zeros(1, device=self.device)
+        self.ghw = torch.zeros_like(self.hw)
+        self.ghb = torch.zeros_like(self.hb)
+        self.convs = [self.e1a, self.e1b, self.e2a, self.e2b, self.e3a, self.e3b, self.d2a,
+                      self.d2b, self.d1a, self.d1b]
+        self.adam: Dict[int, Tuple[torch.Tensor, torch.Tensor]] = {}
+        self.step_count = 0
+        self.buf: Dict[str, torch.Tensor] = {}
+        self.shape = None
+        s = stream_ptr(self.device)
+        for c in self.convs:
+            c.refresh(s)
+
+    def n_params(self) -> int:
+        return sum(c.w.numel() + c.b.numel() for c in self.convs) + self.hw.numel() + 1
+
+    def _alloc(self, n: int, g1):
+        if self.shape == (n, tuple(g1)):
+            return
+        c1, c2, c3 = self.c
+        g2 = half(g1)
+        g3 = half(g2)
+        dev = self.device
+
+        def z(g, c):
+            return torch.zeros((n, *g, c), dtype=BF16, device=dev)
+        b = {}
+        b["e1a"], b["cat1"], b["l2in"] = z(g1, c1), z(g1, c2 + c1), z(g2, c1)
+        b["e2a"], b["cat2"], b["l3in"] = z(g2, c2), z(g2, c3 + c2), z(g3, c2)
+        b["e3a"], b["e3b"] = z(g3, c3), z(g3, c3)
+        b["d2a"], b["d2b"] = z(g2, c2), z(g2, c2)
+        b["d1a"], b["d1b"] = z(g1, c1), z(g1, c1)
+        b["out"] = torch.zeros((n, *g1), dtype=F32, device=dev)
+        for k in ("d1b", "d1a", "cat1", "d2b", "d2a", "cat2", "e3b", "e3a", "l3in", "e2a", "l2in", "e1a"):
+            b["g_" + k] = torch.zeros_like(b[k])
+        b["g_pool2"] = z(g2, c2)
+        b["g_pool1"] = z(g1, c1)
+        self.buf = b
+        self.shape = (n, tuple(g1))
+
+    # ---------------------------------------------------------------- forward
+    def _conv(self, layer: Conv3, x, xoff, y, yoff, relu=True, s=None):
+        call("srf_conv3d_fwd", ptr(x), act(x, xoff), i32(layer.cin), ptr(layer.wb), ptr(layer.b),
+             i32(layer.cout), i32(1 if relu else 0), ptr(y), act(y, yoff), None, s)
+
+    def forward(self, inp: torch.Tensor) -> torch.Tensor:
+        """inp: (N, D, H, W, 16) bfloat16 -> (N, D, H, W) float32."""
+        n, d, h, w, c = inp.shape
+        assert c == self.IN_CH and inp.dtype == BF16
+        self._alloc(n, (d, h, w))
+        self._inp = inp
+        b, s = self.buf, stream_ptr(self.device)
+        c1, c2, c3 = self.c
+        self._conv(self.e1a, inp, 0, b["e1a"], 0, s=s)
+        self._conv(self.e1b, b["e1a"], 0, b["cat1"], c2, s=s)
+        call("srf_cnn_pool2", ptr(b["cat1"]), act(b["cat1"], c2), ptr(b["l2in"]), act(b["l2in"]), i32(c1), i32(0), s)
+        self._conv(self.e2a, b["l2in"], 0, b["e2a"], 0, s=s)
+        self._conv(self.e2b, b["e2a"], 0, b["cat2"], c3, s=s)
+        call("srf_cnn_pool2", ptr(b["cat2"]), act(b["cat2"], c3), ptr(b["l3in"]), act(b["l3in"]), i32(c2), i32(0), s)
+        self._conv(self.e3a, b["l3in"], 0, b["e3a"], 0, s=s)
+        self._conv(self.e3b, b["e3a"], 0, b["e3b"], 0, s=s)
+        call("srf_cnn_upsample2", ptr(b["e3b"]), act(b["e3b"]), ptr(b["cat2"]), act(b["cat2"], 0), i32(c3), i32(0), s)
+        self._conv(self.d2a, b["cat2"], 0, b["d2a"], 0, s=s)
+        self._conv(self.d2b, b["d2a"], 0, b["d2b"], 0, s=s)
+        call("srf_cnn_upsample2", ptr(b["d2b"]), act(b["d2b"]), ptr(b["cat1"]), act(b["cat1"], 0), i32(c2), i32(0), s)
+        self._conv(self.d1a, b["cat1"], 0, b["d1a"], 0, s=s)
+        self._conv(self.d1b, b["d1a"], 0, b["d1b"], 0, s=s)
+        call("srf_cnn_head", ptr(b["d1b"]), act(b["d1b"]), i32(c1), ptr(self.hw), ptr(self.hb),
+             ptr(b["out"]), None, None, None, None, None, s)
+        return b["out"]
+
+    # ---------------------------------------------------------------- backward
+    def _conv_bwd(self, layer: Conv3, x, xoff, y, yoff, gy, gyoff, gx, gxoff, s):
+        """gy: gradient at the layer output (post-ReLU values y); writes gx unless None."""
+        call("srf_cnn_relu_bwd", ptr(gy), act(gy, gyoff), ptr(y), act(y, yoff), i32(layer.cout), s)
+        call("srf_cnn_bias_grad", ptr(gy), act(gy, gyoff), i32(layer.cout), ptr(layer.gb), s)
+        call("srf_conv3d_wgrad", ptr(x), act(x, xoff), i32(layer.cin), ptr(gy), act(gy, gyoff),
+             i32(layer.cout), ptr(layer.gw), s)
+        if gx is not None:
+            call("srf_conv3d_fwd", ptr(gy), act(gy, gyoff), i32(layer.cout), ptr(layer.wf), None,
+                 i32(layer.cin), i32(0), ptr(gx), act(gx, gxoff), None, s)
+
+    def backward(self, gout: torch.Tensor) -> None:
+        """Accumulate parameter gradients for d(loss)/d(out) = gout (N, D, H, W) float32."""
+        b, s = self.buf, stream_ptr(self.device)
+        c1, c2, c3 = self.c
+        call("srf_cnn_head", ptr(b["d1b"]), act(b["d1b"]), i32(c1), ptr(self.hw), ptr(self.hb), None,
+             ptr(gout.contiguous()), ptr(b["g_d1b"]), act(b["g_d1b"]), ptr(self.ghw), ptr(self.ghb), s)
+        self._conv_bwd(self.d1b, b["d1a"], 0, b["d1b"], 0, b["g_d1b"], 0, b["g_d1a"], 0, s)
+        self._conv_bwd(self.d1a, b["cat1"], 0, b["d1a"], 0, b["g_d1a"], 0, b["g_cat1"], 0, s)
+        call("srf_cnn_upsample2", ptr(b["g_d2b"]), act(b["g_d2b"]), ptr(b["g_cat1"]), act(b["g_cat1"], 0), i32(c2), i32(1), s)
+        self._conv_bwd(self.d2b, b["d2a"], 0, b["d2b"], 0, b["g_d2b"], 0, b["g_d2a"], 0, s)
+        self._conv_bwd(self.d2a, b["cat2"], 0, b["d2a"], 0, b["g_d2a"], 0, b["g_cat2"], 0, s)
+        call("srf_cnn_upsample2", ptr(b["g_e3b"]), act(b["g_e3b"]), ptr(b["g_cat2"]), act(b["g_cat2"], 0), i32(c3), i32(1), s)
+        self._conv_bwd(self.e3b, b["e3a"], 0, b["e3b"], 0, b["g_e3b"], 0, b["g_e3a"], 0, s)
+        self._conv_bwd(self.e3a, b["l3in"], 0, b["e3a"], 0, b["g_e3a"], 0, b["g_l3in"], 0, s)
+        # e2b feeds the pool and the skip: gradient = skip slice + pool adjoint
+        call("srf_cnn_pool2", ptr(b["g_pool2"]), act(b["g_pool2"]), ptr(b["g_l3in"]), act(b["g_l3in"]), i32(c2), i32(1), s)
+        call("srf_cnn_add", ptr(b["g_cat2"]), act(b["g_cat2"], c3), ptr(b["g_pool2"]), act(b["g_pool2"]), i32(c2), s)
+        self._conv_bwd(self.e2b, b["e2a"], 0, b["cat2"], c3, b["g_cat2"], c3, b["g_e2a"], 0, s)
+        self._conv_bwd(self.e2a, b["l2in"], 0, b["e2a"], 0, b["g_e2a"], 0, b["g_l2in"], 0, s)
+        call("srf_cnn_pool2", ptr(b["g_pool1"]), act(b["g_pool1"]), ptr(b["g_l2in"]), act(b["g_l2in"]), i32(c1), i32(1), s)
+        call("srf_cnn_add", ptr(b["g_cat1"]), act(b["g_cat1"], c2), ptr(b["g_pool1"]), act(b["g_pool1"]), i32(c1), s)
+        self._conv_bwd(self.e1b, b["e1a"], 0, b["cat1"], c2, b["g_cat1"], c2, b["g_e1a"], 0, s)
+        self._conv_bwd(self.e1a, self._inp, 0, b["e1a"], 0, b["g_e1a"], 0, None, 0, s)
+
+    # ---------------------------------------------------------------- optimiser
+    def zero_grad(self) -> None:
+        for c in self.convs:
+            c.gw.zero_()
+            c.gb.zero_()
+        self.ghw.zero_()
+        self.ghb.zero_()
+
+    def all_params(self) -> List[Tuple[torch.Tensor, torch.Tensor, Optional[torch.Tensor]]]:
+        ps = []
+        for c in self.convs:
+            ps += c.params()
+        ps += [(self.hw, self.ghw, None), (self.hb, self.ghb, None)]
+        return ps
+
+    def step(self, lr: float, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
+        self.step_count += 1
+        s = stream_ptr(self.device)
+        for k, (w, g, bf) in enumerate(self.all_params()):
+            if k not in self.adam:
+                self.adam[k] = (torch.zeros_like(w), torch.zeros_like(w))
+            m, v = self.adam[k]
+            call("srf_cnn_adam", ptr(w), ptr(m), ptr(v), ptr(g), ptr(bf), i64(w.numel()), f32(lr),
+                 f32(b1), f32(b2), f32(eps), i32(self.step_count), s)
+        for c in self.convs:
+            c.refresh(s)
+
+    def loss(self, pred: torch.Tensor, target: torch.Tensor, mask: Optional[torch.Tensor],
+             inv_den: torch.Tensor, grad: Optional[torch.Tensor]) -> torch.Tensor:
+        """Relative squared error averaged over samples (FP64 device scalar); fills its gradient."""
+        out = torch.zeros(1, dtype=torch.float64, device=pred.device)
+        n = pred.shape[0]
+        call("srf_cnn_rel_mse", ptr(pred.contiguous()), ptr(target.contiguous()),
+             ptr(mask.contiguous() if mask is not None else None), ptr(inv_den.contiguous()),
+             i64(pred[0].numel()), i32(n), ptr(grad), ptr(out), stream_ptr(pred.device))
+        return out
+
+
+def upsample_trilinear2(x: torch.Tensor, out_shape) -> torch.Tensor:
+    """(N, d, h, w) float32 -> (N, D, H, W) by trilinear 2x interpolation (srf_cnn_trilinear2)."""
+    n, d, h, w = x.shape
+    D, H, W = out_shape
+    out = torch.empty((n, D, H, W), dtype=F32, device=x.device)
+    call("srf_cnn_trilinear2", ptr(x.contiguous()), i32(n), i32(d), i32(h), i32(w), ptr(out), i32(D),
+         i32(H), i32(W), stream_ptr(x.device))
+    return out
+
+
+def pool_input(full: torch.Tensor) -> torch.Tensor:
+    """(N, D, H, W, 16) bfloat16 at full resolution -> half resolution (srf_cnn_pool2)."""
+    n, d, h, w, c = full.shape
+    g = half((d, h, w))
+    out = torch.empty((n, *g, c), dtype=BF16, device=full.device)
+    call("srf_cnn_pool2", ptr(full), act(full), ptr(out), act(out), i32(c), i32(0), stream_ptr(full.device))
+    return out
+
+
+# ---------------------------------------------------------------- weights
+def save_weights(net: UNet3D, path: str, meta: Dict[str, float]) -> None:
+    """FP32 master weights and metadata (numpy .npz, no pickled objects)."""
+    import numpy as np
+    arrs = {}
+    for name in ("e1a", "e1b", "e2a", "e2b", "e3a", "e3b", "d2a", "d2b", "d1a", "d1b"):
+        c = getattr(net, name)
+        arrs[name + ".w"] = c.w.cpu().numpy()
+        arrs[name + ".b"] = c.b.cpu().numpy()
+    arrs["head.w"] = net.hw.cpu().numpy()
+    arrs["head.b"] = net.hb.cpu().numpy()
+    arrs["channels"] = np.asarray(net.c, np.int64)
+    for k, v in meta.items():
+        arrs["meta." + k] = np.asarray(v, np.float64)
+    np.savez(path, **arrs)
+
+
+def load_weights(path: str, device="cuda") -> Tuple[UNet3D, Dict[str, float]]:
+    import numpy as np
+    z = np.load(path, allow_pickle=False)
+    net = UNet3D(channels=tuple(int(c) for c in z["channels"]), device=device)
+    for name in ("e1a", "e1b", "e2a", "e2b", "e3a", "e3b", "d2a", "d2b", "d1a", "d1b"):
+        c = getattr(net, name)
+        c.w.copy_(torch.as_tensor(z[name + ".w"]))
+        c.b.copy_(torch.as_tensor(z[name + ".b"]))
+        c.wb.copy_(c.w.to(BF16))
+    net.hw.copy_(torch.as_tensor(z["head.w"]))
+    net.hb.copy_(torch.as_tensor(z["head.b"]))
+    s = stream_ptr(net.device)
+    for c in net.convs:
+        c.refresh(s)
+    meta = {k[5:]: float(z[k]) for k in z.files if k.startswith("meta.")}
+    return net, meta
+
+
+DEFAULT_WEIGHTS = __file__.rsplit("/", 1)[0] + "/weights/scatter_unet.npz"
+
+
+# ---------------------------------------------------------------- surrogate with SSS as the judge
+class ScatterSurrogate:
+    """Coarse-sinogram scatter estimate from the network, checked against SSS on a few bins.
+
+    ``estimate(emission, mu)`` returns the flat (51 * 52 * 312) scatter sinogram in SSS units and
+    a record of what happened: the relative L2 difference between the prediction and a fresh SSS
+    on ``spot_bins`` random bins, and whether that exceeded ``fallback_tol`` so that the full SSS
+    was returned instead."""
+
+    def __init__(self, geo, net: UNet3D, target_scale: float, fallback_tol: float = 0.05,
+                 spot_bins: int = 2048, seed: int = 0):
+        self.geo, self.net, self.k = geo, net, float(target_scale)
+        self.fallback_tol, self.spot_bins = fallback_tol, spot_bins
+        self.gen = torch.Generator(device=geo.device).manual_seed(seed)
+
+    @classmethod
+    def load(cls, geo, path: str = DEFAULT_WEIGHTS, **kw) -> "ScatterSurrogate":
+        net, meta = load_weights(path, geo.device)
+        return cls(geo, net, meta["target_scale"], **kw)
+
+    def predict(self, emission: torch.Tensor, mu: torch.Tensor) -> torch.Tensor:
+        from .scatter_sinogram import PAD_GRID, crop_sino, network_input
+        full, scale = network_input(self.geo, emission, mu)
+        out = self.net.forward(pool_input(full))                       # (1, 28, 28, 160)
+        up = upsample_trilinear2(out, PAD_GRID)                          # (1, 56, 56, 320)
+        return crop_sino(up)[0] * (self.k * scale)
+
+    def spot_check(self, emission: torch.Tensor, mu: torch.Tensor, pred: torch.Tensor) -> float:
+        from .scatter_sinogram import sss_sinogram
+        bins = torch.randperm(self.geo.n_bins(), generator=self.gen, device=self.geo.device)[: self.spot_bins]
+        ref = sss_sinogram(self.geo, emission, mu, bins=bins)
+        p = pred.index_select(0, bins)
+        return float((torch.linalg.vector_norm(p - ref) / torch.linalg.vector_norm(ref).clamp_min(1e-30)).item())
+
+    def estimate(self, emission: torch.Tensor, mu: torch.Tensor):
+        from .scatter_sinogram import sss_sinogram
+        pred = self.predict(emission, mu)
+        err = self.spot_check(emission, mu, pred)
+        if not (err <= self.fallback_tol):
+            return sss_sinogram(self.geo, emission, mu), {"spot_rel_l2": err, "fallback": True}
+        return pred, {"spot_rel_l2": err, "fallback": False}
+
+
+# ---------------------------------------------------------------- training
+def build_dataset(geo, seeds, log=None):
+    """Network inputs (N, 28, 28, 160, 16) bf16, targets (N, 28, 28, 160) FP32 in units of each
+    study's emission scale, the scales, and the full-resolution SSS sinograms (N, n_bins)."""
+    from .scatter_sinogram import HALF_GRID, features, network_input, random_phantom, sss_sinogram, target_half
+    n = len(seeds)
+    dev = geo.device
+    X = torch.empty((n, *HALF_GRID, UNet3D.IN_CH), dtype=BF16, device=dev)
+    T = torch.empty((n, *HALF_GRID), dtype=F32, device=dev)
+    S = torch.empty((n, geo.n_bins()), dtype=F32, device=dev)
+    scales = torch.empty(n, dtype=torch.float64)
+    for i, sd in enumerate(seeds):
+        em, mu = random_phantom(int(sd), device=dev)
+        sc = sss_sinogram(geo, em, mu)
+        full, scale = network_input(geo, em, mu, features(geo, em, mu))
+        X[i] = pool_input(full)[0]
+        T[i] = target_half(sc, scale)
+        S[i] = sc
+        scales[i] = scale
+        if log and (i + 1) % 200 == 0:
+            log(f"dataset {i + 1}/{n}")
+    return X, T, scales, S
+
+
+def train(net: UNet3D, X: torch.Tensor, T: torch.Tensor, mask: torch.Tensor, epochs: int,
+          batch: int = 4, lr: float = 2e-3, seed: int = 0, log=None) -> List[float]:
+    """Adam on the masked relative squared error, cosine-decayed learning rate."""
+    n = X.shape[0]
+    g = torch.Generator().manual_seed(seed)
+    inv_den = 1.0 / (T * T * mask).sum(dim=(1, 2, 3)).clamp_min(1e-30)
+    steps = epochs * (n // batch)
+    grad = torch.empty((batch, *T.shape[1:]), dtype=F32, device=X.device)
+    hist, run, k = [], 0.0, 0
+    for ep in range(epochs):
+        perm = torch.randperm(n, generator=g).to(X.device)
+        for j in range(n // batch):
+            idx = perm[j * batch:(j + 1) * batch]
+            frac = k / max(steps - 1, 1)
+            cur = lr * min(1.0, (k + 1) / 100) * 0.5 * (1 + math.cos(math.pi * frac))
+            out = net.forward(X.index_select(0, idx).contiguous())
+            l = net.loss(out, T.index_select(0, idx).contiguous(), mask, inv_den.index_select(0, idx).contiguous(), grad)
+            net.zero_grad()
+            net.backward(grad)
+            net.step(cur)
+            run += float(l.item()) if (k % 50 == 0) else 0.0
+            k += 1
+        hist.append(float(net.loss(net.forward(X[:batch].contiguous()), T[:batch].contiguous(), mask,
+                                   inv_den[:batch].contiguous(), None).item()))
+        if log:
+            log(f"epoch {ep + 1}/{epochs} loss(first batch) {hist[-1]:.5f}")
+    return hist
+
+
+def evaluate(sur: "ScatterSurrogate", seeds) -> List[float]:
+    """Full-resolution relative L2 of the prediction against the full SSS, per held-out seed."""
+    from .scatter_sinogram import random_phantom, sss_sinogram
+    errs = []
+    for sd in seeds:
+        em, mu = random_phantom(int(sd), device=sur.geo.device)
+        ref = sss_sinogram(sur.geo, em, mu)
+        p = sur.predict(em, mu)
+        errs.append(float((torch.linalg.vector_norm(p - ref) / torch.linalg.vector_norm(ref)).item()))
+    return errs
+
+
+def main(argv=None) -> None:
+    """python -m srf_gb300.surrogate --out weights.npz [--train 2000 --held-out 200 --epochs N]"""
+    import argparse
+    import json
+    import time
+    from . import synth
+    from .scatter_sinogram import CoarseGeometry, half_mask
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--train", type=int, default=2000)
+    ap.add_argument("--held-out", type=int, default=200)
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--channels", default="32,64,96")
+    a = ap.parse_args(argv)
+    log = lambda m: print(f"[{time.strftime('%H:%M:%S')}] {m}", flush=True)
+    dev = torch.device("cuda", 0)
+    geo = CoarseGeometry(synth.scanner_clinical(), device=dev)
+    t0 = time.time()
+    X, T, scales, _ = build_dataset(geo, range(a.train), log)
+    torch.cuda.synchronize()
+    log(f"dataset built in {time.time() - t0:.1f} s")
+    mask = half_mask(dev)
+    k = float(((T * mask).sum() / (mask.sum() * T.shape[0])).item())
+    T /= k
+    net = UNet3D(channels=tuple(int(c) for c in a.channels.split(",")), seed=1, device=dev)
+    log(f"parameters {net.n_params()}")
+    t0 = time.time()
+    hist = train(net, X, T, mask, a.epochs, a.batch, a.lr, log=log)
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    del X, T
+    sur = ScatterSurrogate(geo, net, k)
+    errs = evaluate(sur, range(1_000_000, 1_000_000 + a.held_out))
+    meta = {"target_scale": k, "train_studies": a.train, "epochs": a.epochs, "train_s": t_train,
+            "held_out_mean_rel_l2": sum(errs) / len(errs), "held_out_max_rel_l2": max(errs)}
+    save_weights(net, a.out, meta)
+    print(json.dumps({**meta, "loss_history": hist}))
+
+
+if __name__ == "__main__":
+    main()

@@ -73,8 +73,8 @@ def test_argument_checks(lib):
               ctypes.c_float(-1), fake, st, None, None, grid, center, size, fake, None) == 1
     # unknown ratio rule
     assert lib.srf_osem_subset(fake, ctypes.c_int64(5), 7, None, 7, ctypes.c_float(0), ctypes.c_float(0),
-                               ctypes.c_float(0), None, 7, ctypes.c_float(0), fake, None, fake, None,
-                               grid, center, size, None, None) == 1
+                               ctypes.c_float(0), None, None, 7, ctypes.c_float(0), fake, None, fake,
+                               None, grid, center, size, None, None) == 1
     assert b"ratio" in lib.srf_last_error()
     # empty input succeeds without a launch
     assert p(None, ctypes.c_int64(0), 6, fake, st, None, None, grid, center, size, None, None) == 0

@@ -1,0 +1,145 @@
+"""GPU: the surrogate network's BF16 kernels against the float64 CPU oracle (oracle/cnn_oracle.py).
+
+Inputs and weights are drawn as bfloat16 values, so the oracle sees exactly what the tensor cores
+see; the FP32-accumulated results must match to 1e-5 relative, BF16-stored results to BF16
+rounding (4e-3).
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf(a):
+    return torch.as_tensor(a, dtype=torch.float32).to(torch.bfloat16)
+
+
+def _np(t):
+    return t.to(torch.float32).cpu().numpy().astype(np.float64)
+
+
+@pytest.fixture(scope="module")
+def cnn():
+    import cnn_oracle
+    from srf_gb300 import _lib
+    _lib.load()
+    return cnn_oracle
+
+
+def test_conv_forward_dgrad_wgrad(cuda_lib, cnn):
+    from srf_gb300._lib import call, i32, ptr, stream_ptr
+    from srf_gb300.surrogate import act
+    rng = np.random.default_rng(0)
+    dev = torch.device("cuda", 0)
+    n, d, h, w, cin, cout = 2, 5, 6, 7, 32, 48
+    # x lives in a wider buffer at a channel offset (as a U-Net skip slice)
+    xbuf = _bf(rng.standard_normal((n, d, h, w, cin + 16))).to(dev)
+    wt = _bf(rng.standard_normal((cout, 27, cin)) * 0.1).to(dev)
+    bias = torch.as_tensor(rng.standard_normal(cout).astype(np.float32)).to(dev)
+    ybuf = torch.zeros((n, d, h, w, cout + 32), dtype=torch.bfloat16, device=dev)
+    yf = torch.zeros((n, d, h, w, cout + 32), dtype=torch.float32, device=dev)
+    s = stream_ptr(dev)
+    call("srf_conv3d_fwd", ptr(xbuf), act(xbuf, 16), i32(cin), ptr(wt), ptr(bias), i32(cout), i32(1),
+         ptr(ybuf), act(ybuf, 32), ptr(yf), s)
+    x64 = _np(xbuf)[..., 16:]
+    ref = cnn.conv3d(x64, _np(wt), bias.cpu().numpy(), relu=True)
+    got = yf.cpu().numpy()[..., 32:]
+    assert rel_l2(got, ref) <= 1e-5
+    assert rel_l2(_np(ybuf)[..., 32:], ref) <= 4e-3
+    assert np.all(_np(ybuf)[..., :32] == 0)  # nothing written outside the slice
+    # data gradient: the forward kernel on flipped weights
+    dy = _bf(rng.standard_normal((n, d, h, w, cout))).to(dev)
+    wf = torch.empty((cin, 27, cout), dtype=torch.bfloat16, device=dev)
+    call("srf_conv3d_flip_weights", ptr(wt), i32(cout), i32(cin), ptr(wf), s)
+    dxf = torch.zeros((n, d, h, w, cin), dtype=torch.float32, device=dev)
+    dxb = torch.zeros((n, d, h, w, cin), dtype=torch.bfloat16, device=dev)
+    call("srf_conv3d_fwd", ptr(dy), act(dy), i32(cout), ptr(wf), None, i32(cin), i32(0), ptr(dxb),
+         act(dxb), ptr(dxf), s)
+    assert rel_l2(dxf.cpu().numpy(), cnn.conv3d_dgrad(_np(dy), _np(wt))) <= 1e-5
+    # weight gradient (FP32 accumulation, split over voxels)
+    dw = torch.zeros((cout, 27, cin), dtype=torch.float32, device=dev)
+    call("srf_conv3d_wgrad", ptr(xbuf), act(xbuf, 16), i32(cin), ptr(dy), act(dy), i32(cout), ptr(dw), s)
+    assert rel_l2(dw.cpu().numpy(), cnn.conv3d_wgrad(x64, _np(dy))) <= 1e-5
+
+
+def test_pool_upsample_and_adjoints(cuda_lib, cnn):
+    from srf_gb300._lib import call, i32, ptr, stream_ptr
+    from srf_gb300.surrogate import act
+    rng = np.random.default_rng(1)
+    dev = torch.device("cuda", 0)
+    fine = (2, 5, 6, 7, 16)
+    coarse = (2, 3, 3, 4, 16)
+    # multiples of 1/8 with small numerators are exact in bfloat16 and in the sums below
+    x = _bf(rng.integers(-8, 8, fine) / 8.0).to(dev)
+    c = torch.zeros(coarse, dtype=torch.bfloat16, device=dev)
+    s = stream_ptr(dev)
+    call("srf_cnn_pool2", ptr(x), act(x), ptr(c), act(c), i32(16), i32(0), s)
+    assert np.allclose(_np(c), cnn.pool2(_np(x)), atol=1e-2)
+    g = _bf(rng.integers(-8, 8, coarse)).to(dev)
+    gx = torch.zeros(fine, dtype=torch.bfloat16, device=dev)
+    call("srf_cnn_pool2", ptr(gx), act(gx), ptr(g), act(g), i32(16), i32(1), s)
+    assert np.array_equal(_np(gx), cnn.pool2_adjoint(_np(g), fine))
+    u = torch.zeros(fine, dtype=torch.bfloat16, device=dev)
+    call("srf_cnn_upsample2", ptr(g), act(g), ptr(u), act(u), i32(16), i32(0), s)
+    assert np.array_equal(_np(u), cnn.upsample2(_np(g), fine))
+    gc = torch.zeros(coarse, dtype=torch.bfloat16, device=dev)
+    call("srf_cnn_upsample2", ptr(gc), act(gc), ptr(x), act(x), i32(16), i32(1), s)
+    assert np.allclose(_np(gc), cnn.upsample2_adjoint(_np(x), coarse), atol=1e-2)
+
+
+def test_unet_gradient_matches_finite_differences_and_trains(cuda_lib):
+    """Backpropagated gradients of the whole network against central differences of its own
+    forward pass (FP32 head output), and a few Adam steps lowering the loss."""
+    from srf_gb300.surrogate import UNet3D
+    dev = torch.device("cuda", 0)
+    net = UNet3D(channels=(16, 32, 48), seed=3, device=dev)
+    rng = np.random.default_rng(2)
+    n, g = 2, (6, 8, 12)
+    inp = np.zeros((n, *g, 16), np.float32)
+    inp[..., :2] = rng.random((n, *g, 2))
+    inp = _bf(inp).to(dev)
+    target = torch.as_tensor(rng.random((n, *g)).astype(np.float32), device=dev)
+    inv_den = (1.0 / (target ** 2).sum(dim=(1, 2, 3))).contiguous()
+
+    def loss_only():
+        out = net.forward(inp)
+        return float(net.loss(out, target, None, inv_den, None).item())
+
+    out = net.forward(inp)
+    grad = torch.empty_like(out)
+    l0 = float(net.loss(out, target, None, inv_den, grad).item())
+    net.zero_grad()
+    net.backward(grad)
+    # the head bias: exact linear response, gradient = sum of the output gradient
+    gb = float(net.ghb.item())
+    h = 1e-2
+    net.hb += h
+    lp = loss_only()
+    net.hb -= 2 * h
+    lm = loss_only()
+    net.hb += h
+    fd = (lp - lm) / (2 * h)
+    assert abs(fd - gb) <= 1e-3 * max(abs(fd), 1e-6)
+    # a conv bias deep in the network: BF16 activations make FD noisy, so compare direction and size
+    c = net.e2a
+    k = int(torch.argmax(c.gb.abs()))
+    gk = float(c.gb[k])
+    h = 5e-2
+    c.b[k] += h
+    lp = loss_only()
+    c.b[k] -= 2 * h
+    lm = loss_only()
+    c.b[k] += h
+    fd = (lp - lm) / (2 * h)
+    assert np.sign(fd) == np.sign(gk) and abs(fd - gk) <= 0.25 * abs(gk) + 1e-6
+    # training reduces the loss
+    for _ in range(30):
+        out = net.forward(inp)
+        net.loss(out, target, None, inv_den, grad)
+        net.zero_grad()
+        net.backward(grad)
+        net.step(3e-3)
+    assert loss_only() < 0.5 * l0

@@ -105,3 +105,23 @@ def test_osem_tuning_variants_match_oracle(cuda_lib, oracle, small_case, emap_sm
                       tof=True, tof_bin=sc.tof.tof_bin, tof_sigma2=sc.tof.tof_sigma2,
                       tof_nsigma=3.0)
     assert rel_l2(out.data, ref) <= TOL
+
+
+def test_osem_tof_additive_term_matches_oracle(cuda_lib, oracle, small_case, emap_small):
+    """Per-event additive expected counts (a scatter estimate) enter the ratio as y / (p + s)."""
+    import srf_gb300 as nef
+    sc, ic, lors = small_case["scanner"], small_case["ic"], small_case["lors"]
+    lm = nef.Listmode(np.ones(len(lors), np.float32), nef.Lors(lors))
+    em = nef.Emap(emap_small, ic.center, ic.size)
+    add = (np.random.default_rng(8).random(len(lors)) * 1e-3).astype(np.float32)
+    out = nef.OsemFullTof(1, 4, ic, sc, lm, em, tof_nsigma=3.0, seed=2, add=add)()
+    zero = nef.OsemFullTof(1, 4, ic, sc, lm, em, tof_nsigma=3.0, seed=2, add=np.zeros_like(add))()
+    none = nef.OsemFullTof(1, 4, ic, sc, lm, em, tof_nsigma=3.0, seed=2)()
+    assert np.array_equal(zero.data, none.data) or rel_l2(zero.data, none.data) <= 1e-6
+    perm = np.random.default_rng(2).permutation(len(lors))
+    ref = oracle.osem(lors, lm.data, emap_small, ic.shape, ic.center, ic.size, 4, 4, perm,
+                      rule="full_tof", emap_scale=1.0 / 4, guard=True, subset_index="mod",
+                      tof=True, tof_bin=sc.tof.tof_bin, tof_sigma2=sc.tof.tof_sigma2,
+                      tof_nsigma=3.0, add=add)
+    assert rel_l2(out.data, ref) <= TOL
+    assert rel_l2(out.data, none.data) > 1e-4  # the term matters

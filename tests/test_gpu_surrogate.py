@@ -1,0 +1,87 @@
+"""GPU: the learned scatter surrogate (srf_gb300/surrogate.py) against its judge, the
+single-scatter simulation, on phantoms that were not in its training set (training used seeds
+0..1999, these start at 1,000,000).
+
+* the predicted coarse sinogram is within 5 % relative L2 of SSS and passes its own spot check;
+* a network that is wrong is caught by the spot check and SSS is returned instead;
+* TOF OSEM with the surrogate's scatter matches OSEM with SSS scatter within 1 % relative L2,
+  while the image without scatter correction is far off, and the estimate costs >= 10x less time.
+"""
+import statistics
+import time
+
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(u, v):
+    return float((torch.linalg.vector_norm(u - v) / torch.linalg.vector_norm(v)).item())
+
+
+@pytest.fixture(scope="module")
+def geo(cuda_lib):
+    from srf_gb300 import synth
+    from srf_gb300.scatter_sinogram import CoarseGeometry
+    return CoarseGeometry(synth.scanner_clinical(), device=torch.device("cuda", 0))
+
+
+@pytest.fixture(scope="module")
+def sur(geo):
+    from srf_gb300.surrogate import ScatterSurrogate
+    return ScatterSurrogate.load(geo)
+
+
+def test_surrogate_matches_sss_on_held_out_phantoms(geo, sur):
+    from srf_gb300.scatter_sinogram import random_phantom, sss_sinogram
+    for sd in (1_000_100, 1_000_101, 1_000_102):
+        em, mu = random_phantom(sd, device=geo.device)
+        ref = sss_sinogram(geo, em, mu)
+        est, info = sur.estimate(em, mu)
+        assert not info["fallback"], info
+        assert info["spot_rel_l2"] <= 0.05
+        assert rel(est, ref) <= 0.05
+
+
+def test_wrong_network_falls_back_to_sss(geo):
+    from srf_gb300.scatter_sinogram import random_phantom, sss_sinogram
+    from srf_gb300.surrogate import DEFAULT_WEIGHTS, ScatterSurrogate, load_weights
+    net, meta = load_weights(DEFAULT_WEIGHTS, geo.device)
+    net.hb += 3.0  # shifts every prediction far from the SSS sinogram
+    bad = ScatterSurrogate(geo, net, meta["target_scale"])
+    em, mu = random_phantom(1_000_103, device=geo.device)
+    est, info = bad.estimate(em, mu)
+    assert info["fallback"] and info["spot_rel_l2"] > 0.05
+    assert rel(est, sss_sinogram(geo, em, mu)) <= 1e-6
+
+
+def test_surrogate_scatter_osem_matches_sss_scatter_osem_at_a_fraction_of_the_time(geo, sur):
+    from srf_gb300.scatter_sinogram import ScatterStudy, sss_sinogram
+    study = ScatterStudy(geo, 1_000_200, n_trues=1_000_000)
+    em, mu = study.emission, study.mu
+
+    def timed(f):
+        ts = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            f()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts)
+
+    sss_sinogram(geo, em, mu)
+    sur.estimate(em, mu)
+    t_sss = timed(lambda: sss_sinogram(geo, em, mu))
+    t_sur = timed(lambda: sur.estimate(em, mu))
+    est, info = sur.estimate(em, mu)
+    assert not info["fallback"]
+    img_sss = study.reconstruct(study.sss)
+    img_sur = study.reconstruct(est)
+    err = rel(img_sur, img_sss)
+    assert err <= 0.01
+    # what the network buys: the uncorrected image is far from the SSS-corrected one, and the
+    # learned estimate (spot check included) takes a tenth of the time or less
+    assert rel(study.x0, img_sss) >= 5 * err
+    assert t_sss >= 10 * t_sur, (t_sss, t_sur)

@@ -105,3 +105,52 @@ def test_synthetic_events_are_snapped_and_seeded():
     ids = EcatCrystalPosToIndex(sc)(a[:, :3])
     assert np.array_equal(EcatIndexToCrystalPos(sc)(ids), a[:, :3])
     assert abs(float(np.std(a[:, 6])) - 70) < 25  # TOF spread: sigma(d2-d1) = 67.5 mm plus geometry
+
+
+def test_coarse_scatter_geometry_bins_round_trip():
+    import torch
+    from srf_gb300 import synth
+    from srf_gb300.scatter_sinogram import CoarseGeometry, PLANES, RADIAL, VIEWS
+    sc = synth.scanner_clinical()
+    geo = CoarseGeometry(sc, device="cpu")
+    assert geo.vpos.shape == (8112, 3) and geo.n_bins() == (PLANES - 1) * RADIAL * VIEWS
+    assert geo.pairs.min() >= 0 and geo.pairs.max() < 8112
+    # virtual crystals sit between their four crystals: same radius band as the crystals
+    r = np.hypot(geo.vpos[:, 0], geo.vpos[:, 1])
+    assert r.min() > sc.inner_radius and r.max() < sc.outer_radius + 1
+    # an event between crystals of a bin's two virtual crystals maps back to that bin, either order
+    v2f = {}
+    for f, v in enumerate(geo.full_to_virtual):
+        v2f.setdefault(int(v), f)
+    rng = np.random.default_rng(0)
+    picks = rng.choice(geo.n_bins(), 500, replace=False)
+    a = np.array([v2f[int(x)] for x in geo.pairs[picks, 0]])
+    b = np.array([v2f[int(x)] for x in geo.pairs[picks, 1]])
+    ids = torch.as_tensor(np.stack([a, b], 1))
+    assert np.array_equal(geo.event_bins(ids).numpy(), picks)
+    back = geo.event_bins(ids.flip(1)).numpy()
+    assert np.all(back >= 0)
+    same = [sorted(geo.pairs[i]) == sorted(geo.pairs[j]) for i, j in zip(back, picks)]
+    assert all(same)
+    grid = geo.to_grid(torch.arange(geo.n_bins(), dtype=torch.float32))
+    assert grid.shape == (PLANES, RADIAL, VIEWS) and float(grid[-1].abs().sum()) == 0.0
+    # radial bins reach +-300 mm from the axis
+    lors = geo.bin_lors.numpy()
+    p1, p2 = lors[:, :2], lors[:, 3:5]
+    u, w = p2 - p1, -p1
+    d = np.abs(u[:, 0] * w[:, 1] - u[:, 1] * w[:, 0]) / np.linalg.norm(u, axis=1)
+    assert 280 < d.max() < 320
+    # scatter events drawn from a sinogram land in the bins they were drawn from
+    from srf_gb300.scatter_sinogram import sample_scatter_events
+    sino = torch.zeros(geo.n_bins())
+    sino[picks[:20]] = 1.0
+    ev, cid = sample_scatter_events(geo, sino, 4000, seed=1)
+    assert ev.shape == (4000, 7) and cid.shape == (4000, 2)
+    got = geo.event_bins(cid).numpy()
+    hit = np.isin(got, picks[:20])
+    # direct-plane LORs may come back under their equivalent bin (same crystal pair set)
+    for i in np.where(~hit)[0][:50]:
+        j = got[i]
+        assert j >= 0
+        assert any(sorted(geo.pairs[j]) == sorted(geo.pairs[k]) for k in picks[:20])
+    assert hit.mean() > 0.5
