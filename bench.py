@@ -36,6 +36,9 @@ sys.path.insert(0, ROOT)
 METRIC = "TOF OSEM s/iter & LOR-voxel updates/s on 1 GB300 vs plain, rel L2 err ≤1e-5"
 UNIT = "LOR-voxel updates/s"
 FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes (read + write) of one k_osem_subset launch of this workload (2e6 TOF LORs, clinical
+# image), from ncu: profiles/k_osem_subset_tof_clinical_2M_lors.txt
+NCU_TRAFFIC_SUBSET = 124_849_152
 
 
 def parse():
@@ -190,6 +193,30 @@ def cpu_sample_rate(lors_np, x_np, ic, tof, nsigma, threads):
     _, n2 = O.trace(lors_np, ic.shape, ic.center, ic.size, O.RULES_BACK, O.SCATTER, values=r, **kw)
     dt = time.perf_counter() - t0
     return (n1 + n2) / dt, n1 + n2, dt
+
+
+def l2_peaks(dev):
+    """Best-case L2 throughput for 4-byte words on this GPU (srf_calib_l2): loads in GB/s and
+    reductions (red.add.f32) per second over a 32 MB L2-resident buffer, CUDA-event timed."""
+    import torch
+    from srf_gb300._lib import call, i32, i64, ptr, stream_ptr
+    from srf_gb300 import _lib
+    n = 8 << 20
+    buf = torch.zeros(n, dtype=torch.float32, device=dev)
+    sink = torch.zeros(int(_lib.load().srf_calib_sink_size()), dtype=torch.float32, device=dev)
+    s = stream_ptr(dev)
+    stream = torch.cuda.current_stream(dev)
+    out = {}
+    for mode, reps, key in ((0, 40, "read_gbps"), (1, 20, "red_per_s")):
+        call("srf_calib_l2", ptr(buf), i64(n), i32(reps), i32(mode), ptr(sink), s)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call("srf_calib_l2", ptr(buf), i64(n), i32(reps), i32(mode), ptr(sink), s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1000.0
+        out[key] = (n * reps * 4 / sec / 1e9) if mode == 0 else (n * reps / sec)
+    return out
 
 
 def make_workload(a, device, rank):
@@ -529,13 +556,16 @@ def run_surrogate(a, ws, rank, local):
     for _ in range(max(a.warmup, 1)):
         sss_sinogram(geo, em, mu)
         sur.estimate(em, mu)
-    t_sss, t_sur, errs, spot, fallbacks = [], [], [], [], 0
+    t_sss, t_sur, t_pred, t_spot, errs, spot, fallbacks = [], [], [], [], [], [], 0
     clocks = Clocks(local)
     for sd in seeds:
         em, mu = random_phantom(sd, device=dev)
         ts, ref = timed(lambda: sss_sinogram(geo, em, mu))
         tc, (est, info) = timed(lambda: sur.estimate(em, mu))
-        pred = sur.predict(em, mu)
+        tp, pred = timed(lambda: sur.predict(em, mu))
+        tk, _ = timed(lambda: sur.spot_check(em, mu, pred))
+        t_pred.append(tp)
+        t_spot.append(tk)
         errs.append(float((torch.linalg.vector_norm(pred - ref) / torch.linalg.vector_norm(ref)).item()))
         spot.append(info["spot_rel_l2"])
         fallbacks += int(info["fallback"])
@@ -559,6 +589,8 @@ def run_surrogate(a, ws, rank, local):
                        "spot_check_bins": sur.spot_bins, "fallback_tol": sur.fallback_tol,
                        "params": sur.net.n_params()},
             "sss_s_median": med_sss, "surrogate_s_median": med_sur,
+            "predict_s_median": statistics.median(t_pred),
+            "spot_check_s_median": statistics.median(t_spot),
             "sinogram_rel_l2_mean": sum(errs) / len(errs), "sinogram_rel_l2_max": max(errs),
             "spot_rel_l2_mean": sum(spot) / len(spot), "fallbacks": fallbacks,
             "osem": {"events": int(study.events.shape[0]), "scatter_fraction": study.sf,
@@ -669,6 +701,21 @@ def main():
     achieved = alg_bytes / (kern_ms_avg / 1000.0) / 1e9
     peak, peak_kind = peaks()
 
+    # L2 roofline of the same launch: gathers (4 B per projector visit) at the best-case L2 load
+    # rate plus reductions (one per backprojector visit) at the best-case L2 red rate
+    l2 = l2_peaks(dev)
+    t_gather = 4.0 * p_fwd / n_sub / (l2["read_gbps"] * 1e9)
+    t_red = (p_bwd / n_sub) / l2["red_per_s"]
+    t_lor = n_per * stride_b / (peak * 1e9)
+    t_bound = max(t_lor, t_gather + t_red)
+    roofline_l2 = {"bound": "l2 gather + l2 red", "gather_bytes_per_launch": 4.0 * p_fwd / n_sub,
+                   "red_ops_per_launch": p_bwd / n_sub, "l2_read_peak_gbps": l2["read_gbps"],
+                   "l2_red_peak_per_s": l2["red_per_s"], "t_gather_ms": 1000 * t_gather,
+                   "t_red_ms": 1000 * t_red, "t_lor_stream_ms": 1000 * t_lor,
+                   "t_bound_ms": 1000 * t_bound, "launch_ms": kern_ms_avg,
+                   "frac": 1000 * t_bound / kern_ms_avg,
+                   "peaks": "measured in this run (srf_calib_l2, 32 MB buffer)"}
+
     # end to end through the public API: pinned host LORs -> device -> one iteration -> image back
     e2e = None
     if not a.no_e2e:
@@ -720,10 +767,12 @@ def main():
             "updates_per_iter": updates_per_iter, "pairs_fwd": p_fwd, "pairs_bwd": p_bwd,
             "emap_s": emap_s, "emap_lors": int(sc.nb_crystals) ** 2,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": NCU_TRAFFIC_SUBSET if (n_per == 2_000_000 and a.nsigma == 3.0) else None,
                          "kernel": "k_osem_subset (fused projection+ratio+backprojection)",
                          "launch_ms": kern_ms_avg, "alg_bytes_per_launch": alg_bytes,
                          "peak_kind": peak_kind},
+            "roofline_l2": roofline_l2,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": a.steps * n_sub * 2,
         }

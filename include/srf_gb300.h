@@ -194,8 +194,10 @@ typedef struct srf_study {
 } srf_study;
 
 /* srf_osem_subset for every study at once: a persistent kernel walks all studies' 32-LOR batches.
- * batch_offsets (device, n_studies + 1): study s owns batches [off[s], off[s + 1]),
- * off[s + 1] - off[s] = ceil(n_s / 32); total_batches = off[n_studies]. */
+ * batch_offsets (device, n_studies + 3 int64): study s owns batches [off[s], off[s + 1]),
+ * off[s + 1] - off[s] = ceil(n_s / 32); total_batches = off[n_studies]. The two entries after
+ * off[n_studies] are the kernel's work counters: zero them once when the array is made; every
+ * launch leaves them at zero again. Launches sharing one array must be ordered (one stream). */
 int srf_osem_subset_batch(const srf_study *studies, int32_t n_studies,
                           const int64_t *batch_offsets, int64_t total_batches, int32_t use_tof,
                           float tof_bin, float tof_sigma2, float tof_nsigma, int32_t ratio_rule,
@@ -267,6 +269,14 @@ int srf_sss(const int32_t *pairs, int64_t n_pairs, const float *crystal_pos, int
             const int32_t grid_block[3], int32_t low_energy, int32_t high_energy,
             float resolution, float *scatter, float *scale, void *stream);
 
+/* ------------------------------------------------------------------ L2 calibration */
+/* No counterpart in the reference: best-case L2 throughput for 4-byte words, the denominators of
+ * the gather and atomic rooflines. mode 0: reps passes of loads over buf[0, n) (sink receives
+ * srf_calib_sink_size() floats); mode 1: reps passes of buf[i] += 1 as reductions. Keep n * 4 B
+ * well below the L2 size and time the call on `stream`. */
+int srf_calib_l2(float *buf, int64_t n, int32_t reps, int32_t mode, float *sink, void *stream);
+int srf_calib_sink_size(void);
+
 /* ------------------------------------------------------------------ scatter surrogate network */
 /* BF16 3-D U-Net building blocks with FP32 accumulation (not in the reference). Activations are
  * NDHWC bfloat16 described by int32[6] = {n, d, h, w, channel_stride, channel_offset} so a layer
@@ -291,18 +301,19 @@ int srf_cnn_pool2(const void *fine, const int32_t fs[6], void *coarse, const int
 /* nearest 2x upsampling coarse -> fine (adjoint: fine gradient summed into coarse). */
 int srf_cnn_upsample2(const void *coarse, const int32_t cs[6], void *fine, const int32_t fs[6], int32_t c,
                       int32_t adjoint, void *stream);
+/* Sub-voxel 1x1x1 head: 8 FP32 outputs per coarse voxel (z, y, x), output q = 4i + 2j + k written
+   to fine voxel (2z + i, 2y + j, 2x + k) of out (n, fine[0], fine[1], fine[2]), fine <= 2 x coarse:
+   out = b[q] + sum_c x[v, c] w[q * c + c']. With gout != NULL: gx (optional) = data gradient,
+   gw[8][c] and gb[8] accumulate the parameter gradients. */
+int srf_cnn_head8(const void *x, const int32_t xs[6], int32_t c, const float *w, const float *b, float *out,
+                  const int32_t fine[3], const float *gout, void *gx, const int32_t gs[6], float *gw,
+                  float *gb, void *stream);
 /* dst slice += src slice. */
 int srf_cnn_add(void *dst, const int32_t ds[6], const void *src, const int32_t ss[6], int32_t c, void *stream);
-/* 1x1x1 head to one FP32 channel: forward when gout == NULL, else gradients (gx, gw, gb). */
-int srf_cnn_head(const void *x, const int32_t xs[6], int32_t c, const float *w, const float *b, float *out,
-                 const float *gout, void *gx, const int32_t gs[6], float *gw, float *gb, void *stream);
 /* *loss += (1/n_samples) sum_s sum_i m (p - t)^2 inv_den[s] (FP64); grad = its gradient,
    2 m (p - t) inv_den[s] / n_samples. */
 int srf_cnn_rel_mse(const float *pred, const float *target, const float *mask, const float *inv_den,
                     int64_t per_sample, int32_t n_samples, float *grad, double *loss, void *stream);
-/* trilinear 2x upsampling of single-channel FP32 volumes (n, d, h, w) -> (n, D, H, W). */
-int srf_cnn_trilinear2(const float *src, int32_t n, int32_t d, int32_t h, int32_t w, float *dst, int32_t D,
-                       int32_t H, int32_t W, void *stream);
 /* Adam step on FP32 parameters, refreshing an optional BF16 copy. */
 int srf_cnn_adam(float *w, float *m, float *v, const float *g, void *bf16_copy, int64_t n, float lr,
                  float b1, float b2, float eps, int32_t step, void *stream);

@@ -76,3 +76,28 @@ def upsample2_adjoint(g, coarse_shape):
     gp = np.zeros((n, 2 * D, 2 * H, 2 * W, c))
     gp[:, :g.shape[1], :g.shape[2], :g.shape[3]] = g
     return gp.reshape(n, D, 2, H, 2, W, 2, c).sum(axis=(2, 4, 6))
+
+
+def head8(x, w, b, fine):
+    """Sub-voxel head: out[n, 2z+i, 2y+j, 2x+k] = b[q] + x[n, z, y, x] . w[q], q = 4i + 2j + k,
+    cropped to the fine grid."""
+    x = np.asarray(x, np.float64)
+    n, d, h, ww, c = x.shape
+    o = np.einsum("ndhwc,qc->ndhwq", x, np.asarray(w, np.float64)) + np.asarray(b, np.float64)
+    full = o.reshape(n, d, h, ww, 2, 2, 2).transpose(0, 1, 4, 2, 5, 3, 6).reshape(n, 2 * d, 2 * h, 2 * ww)
+    D, H, W = fine
+    return full[:, :D, :H, :W]
+
+
+def head8_grads(x, w, gout):
+    """(gx, gw, gb) of head8 for the fine-grid gradient gout."""
+    x = np.asarray(x, np.float64)
+    n, d, h, ww, c = x.shape
+    D, H, W = gout.shape[1:]
+    gp = np.zeros((n, 2 * d, 2 * h, 2 * ww))
+    gp[:, :D, :H, :W] = gout
+    gq = gp.reshape(n, d, 2, h, 2, ww, 2).transpose(0, 1, 3, 5, 2, 4, 6).reshape(n, d, h, ww, 8)
+    gx = gq @ np.asarray(w, np.float64)
+    gw = np.einsum("ndhwq,ndhwc->qc", gq, x)
+    gb = gq.sum(axis=(0, 1, 2, 3))
+    return gx, gw, gb

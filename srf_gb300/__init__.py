@@ -11,11 +11,12 @@ from .geometry import (Block, EcatCrystalPosToIndex, EcatIndexToCrystalPos, Imag
 from .functions import BackProject, BackProjectTof, Project, ProjectTof
 from .emap_generator import EcatEmapGenerator, EmapGenerator
 from .recon import Mlem, MlemFull, MlemFullTof, OsemFull, OsemFullTof
+from .scatter import AttenuationCorrect, ScatterCorrect, UmapProject
 
 __all__ = [
     "Emap", "Image", "Listmode", "Lors", "Umap", "Block", "EcatCrystalPosToIndex",
     "EcatIndexToCrystalPos", "ImageConfig", "LorsToListmode", "PetEcatListmodeTrans",
     "PetEcatScanner", "TofConfig", "BackProject", "BackProjectTof", "Project", "ProjectTof",
     "EcatEmapGenerator", "EmapGenerator", "Mlem", "MlemFull", "MlemFullTof", "OsemFull",
-    "OsemFullTof",
+    "OsemFullTof", "AttenuationCorrect", "ScatterCorrect", "UmapProject",
 ]

@@ -291,45 +291,112 @@ __global__ void k_upsample2(const __nv_bfloat16 *__restrict__ src, Act sa, __nv_
     }
 }
 
-// 1x1x1 head: out[v] = b + sum_c x[v, c] w[c] (FP32 out), and its gradients
-__global__ void k_head_fwd(const __nv_bfloat16 *__restrict__ x, Act xa, int c, const float *__restrict__ w,
-                           const float *__restrict__ bp, float *__restrict__ out, int64_t nvox_total) {
-    const float b = bp ? *bp : 0.0f;
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nvox_total; v += (int64_t)gridDim.x * blockDim.x) {
-        float s = b;
-        for (int ch = 0; ch < c; ++ch) s = fmaf(__bfloat162float(x[v * xa.cstride + xa.coff + ch]), w[ch], s);
-        out[v] = s;
+// Sub-voxel head: 8 FP32 outputs per coarse voxel v = (z, y, x), output q = 4i + 2j + k landing at
+// fine voxel (2z + i, 2y + j, 2x + k) of an (n, D, H, W) grid (outputs past D/H/W are dropped):
+// out = b[q] + sum_c x[v, c] w[q][c]. Weights [8][c] FP32, c <= 64. Voxel counts are below 2^31
+// (checked on the host), so the index arithmetic is 32-bit.
+struct Fine {
+    int64_t base;      // fine offset of sub-voxel (0, 0, 0)
+    int lim;           // bit q set when sub-voxel q lies inside the fine grid
+};
+
+__device__ __forceinline__ Fine fine_of(int v, const Act &xa, int D, int H, int W) {
+    int r = v;
+    const int x = r % xa.w; r /= xa.w;
+    const int y = r % xa.h; r /= xa.h;
+    const int z = r % xa.d;
+    const int nb = r / xa.d;
+    Fine f;
+    f.base = (((int64_t)nb * D + 2 * z) * H + 2 * y) * (int64_t)W + 2 * x;
+    const bool zi = 2 * z + 1 < D, yi = 2 * y + 1 < H, xi = 2 * x + 1 < W;
+    f.lim = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        if ((!(q & 4) || zi) && (!(q & 2) || yi) && (!(q & 1) || xi)) f.lim |= 1 << q;
+    return f;
+}
+
+__device__ __forceinline__ int64_t fine_off(const Fine &f, int q, int H, int W) {
+    return f.base + ((int64_t)(q >> 2) * H + ((q >> 1) & 1)) * W + (q & 1);
+}
+
+__global__ void k_head8_fwd(const __nv_bfloat16 *__restrict__ x, Act xa, int c, const float *__restrict__ w,
+                            const float *__restrict__ bp, float *__restrict__ out, int D, int H, int W,
+                            int nvox_total) {
+    __shared__ float sw[8][64];
+    __shared__ float sb[8];
+    for (int t = threadIdx.x; t < 8 * 64; t += blockDim.x) sw[t >> 6][t & 63] = (t & 63) < c ? w[(t >> 6) * c + (t & 63)] : 0.0f;
+    if (threadIdx.x < 8) sb[threadIdx.x] = bp ? bp[threadIdx.x] : 0.0f;
+    __syncthreads();
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nvox_total; v += gridDim.x * blockDim.x) {
+        float acc[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[q] = sb[q];
+        const __nv_bfloat16 *xr = x + (int64_t)v * xa.cstride + xa.coff;
+        for (int ch = 0; ch < c; ++ch) {
+            const float xv = __bfloat162float(xr[ch]);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc[q] = fmaf(xv, sw[q][ch], acc[q]);
+        }
+        const Fine f = fine_of(v, xa, D, H, W);
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (f.lim >> q & 1) out[fine_off(f, q, H, W)] = acc[q];
     }
 }
 
-__global__ void k_head_bwd(const __nv_bfloat16 *__restrict__ x, Act xa, int c, const float *__restrict__ w,
-                           const float *__restrict__ gout, __nv_bfloat16 *__restrict__ gx, Act ga,
-                           float *__restrict__ gw, float *__restrict__ gb, int64_t nvox_total) {
-    __shared__ float sw[64];
-    __shared__ float sgw[64];
-    __shared__ float sgb;
-    for (int t = threadIdx.x; t < 64; t += blockDim.x) {
-        sw[t] = t < c ? w[t] : 0.0f;
-        sgw[t] = 0.0f;
-    }
-    if (threadIdx.x == 0) sgb = 0.0f;
+// gx[v, ch] = sum_q gout[fine(v, q)] w[q][ch]; one thread per (voxel, channel)
+__global__ void k_head8_dx(const float *__restrict__ gout, Act xa, int c, const float *__restrict__ w,
+                           __nv_bfloat16 *__restrict__ gx, Act ga, int D, int H, int W, int64_t total) {
+    __shared__ float sw[8][64];
+    for (int t = threadIdx.x; t < 8 * 64; t += blockDim.x) sw[t >> 6][t & 63] = (t & 63) < c ? w[(t >> 6) * c + (t & 63)] : 0.0f;
     __syncthreads();
-    float lgw[64];
-    for (int ch = 0; ch < 64; ++ch) lgw[ch] = 0.0f;
-    float lgb = 0.0f;
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nvox_total; v += (int64_t)gridDim.x * blockDim.x) {
-        const float g = gout[v];
-        lgb += g;
-        for (int ch = 0; ch < c; ++ch) {
-            lgw[ch] = fmaf(g, __bfloat162float(x[v * xa.cstride + xa.coff + ch]), lgw[ch]);
-            gx[v * ga.cstride + ga.coff + ch] = __float2bfloat16(g * sw[ch]);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int v = (int)(i / c);
+        const int ch = (int)(i - (int64_t)v * c);
+        const Fine f = fine_of(v, xa, D, H, W);
+        float s = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (f.lim >> q & 1) s = fmaf(gout[fine_off(f, q, H, W)], sw[q][ch], s);
+        gx[(int64_t)v * ga.cstride + ga.coff + ch] = __float2bfloat16(s);
+    }
+}
+
+// gw[q][ch] += sum_v gout[fine(v, q)] x[v, ch], gb[q] += sum_v gout[fine(v, q)]. A block takes
+// `chunk` voxels: their 8 sub-voxel gradients are staged in shared memory, then thread t owns
+// the pairs (q, ch) = divmod(t + k * blockDim, c + 1) (ch == c is the bias) and adds one atomic
+// per pair.
+constexpr int kHeadChunk = 128;
+
+__global__ void k_head8_dw(const __nv_bfloat16 *__restrict__ x, Act xa, int c, const float *__restrict__ gout,
+                           float *__restrict__ gw, float *__restrict__ gb, int D, int H, int W, int nvox_total) {
+    __shared__ float sg[kHeadChunk][8];
+    const int v0 = blockIdx.x * kHeadChunk;
+    const int nv = min(kHeadChunk, nvox_total - v0);
+    for (int t = threadIdx.x; t < kHeadChunk * 8; t += blockDim.x) {
+        const int j = t >> 3, q = t & 7;
+        float g = 0.0f;
+        if (j < nv) {
+            const Fine f = fine_of(v0 + j, xa, D, H, W);
+            if (f.lim >> q & 1) g = gout[fine_off(f, q, H, W)];
+        }
+        sg[j][q] = g;
+    }
+    __syncthreads();
+    const int pairs = 8 * (c + 1);
+    for (int t = threadIdx.x; t < pairs; t += blockDim.x) {
+        const int q = t / (c + 1), ch = t - q * (c + 1);
+        float s = 0.0f;
+        if (ch < c) {
+            const __nv_bfloat16 *xr = x + (int64_t)v0 * xa.cstride + xa.coff + ch;
+            for (int j = 0; j < nv; ++j) s = fmaf(sg[j][q], __bfloat162float(xr[(int64_t)j * xa.cstride]), s);
+            atomicAdd(gw + q * c + ch, s);
+        } else {
+            for (int j = 0; j < nv; ++j) s += sg[j][q];
+            atomicAdd(gb + q, s);
         }
     }
-    for (int ch = 0; ch < c; ++ch) atomicAdd(&sgw[ch], lgw[ch]);
-    atomicAdd(&sgb, lgb);
-    __syncthreads();
-    for (int t = threadIdx.x; t < c; t += blockDim.x) atomicAdd(gw + t, sgw[t]);
-    if (threadIdx.x == 0) atomicAdd(gb, sgb);
 }
 
 // Adam on FP32 masters, refreshed BF16 copy (bf may be NULL for FP32-only parameters)
@@ -376,32 +443,6 @@ __global__ void k_rel_mse(const float *__restrict__ pred, const float *__restric
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(loss, acc);
-}
-
-// trilinear 2x upsampling of a single-channel FP32 volume (cell-centred samples)
-__global__ void k_trilinear2(const float *__restrict__ src, int n, int d, int h, int w, float *__restrict__ dst,
-                             int D, int H, int W) {
-    const int64_t total = (int64_t)n * D * H * W;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        int64_t v = i;
-        const int ox = (int)(v % W); v /= W;
-        const int oy = (int)(v % H); v /= H;
-        const int oz = (int)(v % D);
-        const int64_t nb = v / D;
-        const float fz = fminf(fmaxf((oz + 0.5f) * 0.5f - 0.5f, 0.0f), (float)(d - 1));
-        const float fy = fminf(fmaxf((oy + 0.5f) * 0.5f - 0.5f, 0.0f), (float)(h - 1));
-        const float fx = fminf(fmaxf((ox + 0.5f) * 0.5f - 0.5f, 0.0f), (float)(w - 1));
-        const int z0 = (int)fz, y0 = (int)fy, x0 = (int)fx;
-        const int z1 = min(z0 + 1, d - 1), y1 = min(y0 + 1, h - 1), x1 = min(x0 + 1, w - 1);
-        const float az = fz - z0, ay = fy - y0, ax = fx - x0;
-        const float *b = src + nb * (int64_t)d * h * w;
-        auto at = [&](int z, int y, int x) { return b[((int64_t)z * h + y) * w + x]; };
-        const float c00 = at(z0, y0, x0) * (1 - ax) + at(z0, y0, x1) * ax;
-        const float c01 = at(z0, y1, x0) * (1 - ax) + at(z0, y1, x1) * ax;
-        const float c10 = at(z1, y0, x0) * (1 - ax) + at(z1, y0, x1) * ax;
-        const float c11 = at(z1, y1, x0) * (1 - ax) + at(z1, y1, x1) * ax;
-        dst[i] = ((c00 * (1 - ay) + c01 * ay) * (1 - az) + (c10 * (1 - ay) + c11 * ay) * az);
-    }
 }
 
 inline int check_act(const Act &a, int c, const char *name) {
@@ -520,23 +561,36 @@ int srf_cnn_upsample2(const void *coarse, const int32_t cs[6], void *fine, const
     return check_cuda("upsample launch");
 }
 
-int srf_cnn_head(const void *x, const int32_t xs[6], int32_t c, const float *w, const float *b, float *out,
-                 const float *gout, void *gx, const int32_t gs[6], float *gw, float *gb, void *stream) {
+int srf_cnn_head8(const void *x, const int32_t xs[6], int32_t c, const float *w, const float *b, float *out,
+                  const int32_t fine[3], const float *gout, void *gx, const int32_t gs[6], float *gw,
+                  float *gb, void *stream) {
     if (c <= 0 || c > 64) return fail(SRF_EINVAL, "head supports 1..64 channels");
+    if (!x || !xs || !w || !fine) return fail(SRF_EINVAL, "x, xs, w and fine must not be NULL");
     const Act xa = act_of(xs);
     int rc;
     if ((rc = check_act(xa, c, "x"))) return rc;
+    const int D = fine[0], H = fine[1], W = fine[2];
+    if (D <= 0 || H <= 0 || W <= 0 || D > 2 * xa.d || H > 2 * xa.h || W > 2 * xa.w)
+        return fail(SRF_EGRID, "fine grid must be within twice the coarse grid");
     const int64_t nv = (int64_t)xa.n * xa.d * xa.h * xa.w;
+    if (nv >= (int64_t(1) << 31)) return fail(SRF_ERANGE, "head8 supports fewer than 2^31 voxels");
     cudaStream_t s = (cudaStream_t)stream;
     if (!gout) {
-        k_head_fwd<<<grid_for(k_head_fwd, nv, 256), 256, 0, s>>>((const __nv_bfloat16 *)x, xa, c, w, b, out, nv);
-    } else {
+        if (!out) return fail(SRF_EINVAL, "out must not be NULL");
+        k_head8_fwd<<<grid_for(k_head8_fwd, nv, 256), 256, 0, s>>>((const __nv_bfloat16 *)x, xa, c, w, b, out, D, H, W, (int)nv);
+        return check_cuda("head8 launch");
+    }
+    if (gx) {
         const Act ga = act_of(gs);
         if ((rc = check_act(ga, c, "gx"))) return rc;
-        unsigned blocks = (unsigned)std::min<int64_t>((nv + 255) / 256, (int64_t)num_sms() * 4);
-        k_head_bwd<<<blocks, 256, 0, s>>>((const __nv_bfloat16 *)x, xa, c, w, gout, (__nv_bfloat16 *)gx, ga, gw, gb, nv);
+        if (ga.n != xa.n || ga.d != xa.d || ga.h != xa.h || ga.w != xa.w) return fail(SRF_EGRID, "gx shape differs from x");
+        k_head8_dx<<<grid_for(k_head8_dx, nv * c, 256), 256, 0, s>>>(gout, xa, c, w, (__nv_bfloat16 *)gx, ga, D, H, W, nv * c);
     }
-    return check_cuda("head launch");
+    if (gw && gb) {
+        const int64_t blocks = (nv + kHeadChunk - 1) / kHeadChunk;
+        k_head8_dw<<<(unsigned)blocks, 288, 0, s>>>((const __nv_bfloat16 *)x, xa, c, gout, gw, gb, D, H, W, (int)nv);
+    }
+    return check_cuda("head8 gradient launch");
 }
 
 int srf_cnn_add(void *dst, const int32_t ds[6], const void *src, const int32_t ss[6], int32_t c, void *stream) {
@@ -555,14 +609,6 @@ int srf_cnn_rel_mse(const float *pred, const float *target, const float *mask, c
     k_rel_mse<<<grid_for(k_rel_mse, per_sample * n_samples, 256), 256, 0, (cudaStream_t)stream>>>(
         pred, target, mask, inv_den, per_sample, n_samples, grad, loss);
     return check_cuda("loss launch");
-}
-
-int srf_cnn_trilinear2(const float *src, int32_t n, int32_t d, int32_t h, int32_t w, float *dst, int32_t D,
-                       int32_t H, int32_t W, void *stream) {
-    if (!src || !dst || n <= 0 || d <= 0 || h <= 0 || w <= 0 || D <= 0 || H <= 0 || W <= 0) return fail(SRF_EINVAL, "bad arguments");
-    const int64_t t = (int64_t)n * D * H * W;
-    k_trilinear2<<<grid_for(k_trilinear2, t, 256), 256, 0, (cudaStream_t)stream>>>(src, n, d, h, w, dst, D, H, W);
-    return check_cuda("trilinear launch");
 }
 
 int srf_cnn_adam(float *w, float *m, float *v, const float *g, void *bf16_copy, int64_t n, float lr,

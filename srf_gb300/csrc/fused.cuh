@@ -19,23 +19,27 @@
 namespace srf {
 
 // Per-LOR record in shared memory: everything the slab loop needs, computed once per LOR by one
-// lane (setup_rec) and read by the LOR's group as six 16-byte broadcasts.
+// lane (setup_rec) and read by the LOR's group as seven 16-byte broadcasts.
 struct __align__(16) LorRec {
     float p1, p2, q1, z1;
-    float kq, kz, wc, invL2;
+    float kq, kz, wc, invL2;     // wc includes the TOF amplitude
     float ratio1, L, yv, pd;
-    float inv_pd, Aq, Bq, Az;  // fast forms: boundary(pp) ~= fmaf(B, pp, A)
-    float Bz, mq, mz, ad;      // mq, mz: floor margins of the fast forms; ad: additive term
-    int lo, hi, flags, pad1;
+    float tA, Aq, Bq, Az;        // fast forms: boundary(pp) ~= fmaf(B, pp, A); TOF d(ip) ~= fmaf(tA, ip, tB)
+    float Bz, mq, mz, ad;        // mq, mz: floor margins of the fast forms; ad: additive term
+    int lo, hi, flags, pmlo;     // [pmlo, pmhi]: slabs the projector's endpoint rule keeps
+    int pmhi;
+    float tB, invq, invz;        // invq, invz: 1 / (boundary step per slab) of q and z
 };
 constexpr int F_VALID = 1, F_PROJ = 2, F_XDOM = 4, F_TIE = 8;
+constexpr int kRecVec = sizeof(LorRec) / 16;
+static_assert(sizeof(LorRec) == 112, "LorRec is seven 16-byte vectors");
 
 __device__ __forceinline__ LorRec load_rec(const LorRec *src) {
     LorRec R;
     const float4 *s4 = reinterpret_cast<const float4 *>(src);
     float4 *d4 = reinterpret_cast<float4 *>(&R);
 #pragma unroll
-    for (int c = 0; c < 6; ++c) d4[c] = s4[c];
+    for (int c = 0; c < kRecVec; ++c) d4[c] = s4[c];
     return R;
 }
 
@@ -43,15 +47,21 @@ __device__ __forceinline__ void store_rec(LorRec *dst, const LorRec &R) {
     const float4 *s4 = reinterpret_cast<const float4 *>(&R);
     float4 *d4 = reinterpret_cast<float4 *>(dst);
 #pragma unroll
-    for (int c = 0; c < 6; ++c) d4[c] = s4[c];
+    for (int c = 0; c < kRecVec; ++c) d4[c] = s4[c];
 }
+
+// Relative margin on the TOF truncation test t2 <= nsigma^2 (fast t2 is within ~1e-5 relative).
+constexpr float kTruncMargin = 2e-4f;
 
 // grid-wide constants, rounded exactly as in setup_lor
 struct GridK {
     float dx_, dy, dz, nx2, ny2, nz2;
     float tof_bin_, expand, inv_expand, tof_amp, nsig2, nsw;  // nsw = nsigma * sqrt(expand)
+    float k2, e2cut, e2tol;  // fast TOF: e2 = d^2 k2 = -t2 log2(e) / 2; kept when e2 >= e2cut
     bool dy_one;
 };
+
+constexpr float kHalfLog2e = 0.72134752044448170f;  // log2(e) / 2: exp(-t2 / 2) = exp2(-t2 * this)
 
 template <bool TOF>
 __device__ __forceinline__ GridK make_gridk(const Grid &g, const TofParams &tp) {
@@ -64,6 +74,7 @@ __device__ __forceinline__ GridK make_gridk(const Grid &g, const TofParams &tp) 
     k.nz2 = __fdiv_rn((float)g.nz, 2.0f);
     k.dy_one = (k.dy == 1.0f);
     k.tof_bin_ = k.expand = k.inv_expand = k.tof_amp = k.nsig2 = k.nsw = 0.0f;
+    k.k2 = k.e2cut = k.e2tol = 0.0f;
     if (TOF) {
         k.tof_bin_ = __fdiv_rn(tp.tof_bin, k.dx_);
         const float s2 = __fdiv_rn(__fdiv_rn(tp.tof_sigma2, k.dx_), k.dx_);
@@ -72,8 +83,51 @@ __device__ __forceinline__ GridK make_gridk(const Grid &g, const TofParams &tp) 
         k.tof_amp = k.tof_bin_ * rsqrtf(2.0f * 3.1415926f * k.expand);
         k.nsig2 = tp.nsigma * tp.nsigma;
         k.nsw = tp.nsigma * sqrtf(k.expand);
+        k.k2 = -kHalfLog2e * k.inv_expand;
+        k.e2cut = -kHalfLog2e * k.nsig2;
+        k.e2tol = kTruncMargin * kHalfLog2e * k.nsig2;
     }
     return k;
+}
+
+// The projector's endpoint slab rule at slab ip (pp1 = ip - np/2, pp2 = pp1 + 1, both exact):
+// non-TOF keeps slabs up to endpoint 2 (siddon.cu.cc:56-57), TOF keeps slabs from endpoint 1 on
+// (siddon_tof.cu.cc:68-75 for x, :228-235 for y, with their different strictness).
+__device__ __forceinline__ bool proj_rule_at(float p1, float p2, bool xdom, bool tof, int ip, float np2) {
+    const float pp1 = __fsub_rn((float)ip, np2);
+    const float pp2 = __fadd_rn(pp1, 1.0f);
+    if (!tof) return !((p1 < p2 && pp2 > p2) || (p1 >= p2 && pp1 < p2));
+    if (xdom) return !((p2 > p1 && pp1 <= p1) || (p2 < p1 && pp2 >= p1));
+    return !((p2 > p1 && pp1 < p1) || (p2 < p1 && pp2 > p1));
+}
+
+// The rule keeps a contiguous slab range [pmlo, pmhi] (one side open): the bound is estimated in
+// double and then settled with the float predicate itself, so the range is exactly the rule's.
+__device__ __forceinline__ void proj_slab_range(float p1, float p2, bool xdom, bool tof, float np2, int np,
+                                                int &pmlo, int &pmhi) {
+    pmlo = -2;
+    pmhi = np + 1;
+    const double a1 = (double)p1 + (double)np2, a2 = (double)p2 + (double)np2;
+    int upper = 0;  // +1: rule keeps ip <= bound; -1: keeps ip >= bound; 0: keeps every slab
+    double est = 0.0;
+    if (!tof) {
+        if (p1 < p2) { upper = 1; est = floor(a2 - 1.0); } else { upper = -1; est = ceil(a2); }
+    } else if (p2 > p1) {
+        upper = -1; est = xdom ? floor(a1) + 1.0 : ceil(a1);
+    } else if (p2 < p1) {
+        upper = 1; est = xdom ? ceil(a1 - 1.0) - 1.0 : floor(a1 - 1.0);
+    }
+    if (upper == 0) return;
+    int b = (int)fmin(fmax(est, -2.0), (double)np + 1.0);
+    if (upper > 0) {
+        for (int t = 0; t < 4 && b < np + 1 && proj_rule_at(p1, p2, xdom, tof, b + 1, np2); ++t) ++b;
+        for (int t = 0; t < 4 && b > -2 && !proj_rule_at(p1, p2, xdom, tof, b, np2); ++t) --b;
+        pmhi = b;
+    } else {
+        for (int t = 0; t < 4 && b > -2 && proj_rule_at(p1, p2, xdom, tof, b - 1, np2); ++t) --b;
+        for (int t = 0; t < 4 && b < np + 1 && !proj_rule_at(p1, p2, xdom, tof, b, np2); ++t) ++b;
+        pmlo = b;
+    }
 }
 
 // Lane-parallel setup of one LOR (both rule sets). Rounding of every value that feeds a floor or
@@ -144,15 +198,25 @@ __device__ __forceinline__ LorRec setup_rec(const float *l, float tv, float yv, 
     // S = (|k| (|p1| + np) + |a|) / d + |n2| + 2 over the LOR's slabs; 2^-20 * S bounds their
     // difference with room to spare.
     R.pd = pd;
-    R.inv_pd = 1.0f / pd;
     R.Bq = R.kq / dq;
     R.Aq = (R.q1 - R.kq * R.p1) / dq + nq2;
     R.Bz = R.kz / k.dz;
     R.Az = (z1 - R.kz * R.p1) / k.dz + k.nz2;
+    R.invq = 1.0f / fabsf(R.Bq);  // inf when q never steps (then unused)
+    R.invz = 1.0f / fabsf(R.Bz);
     const float e = 9.5367431640625e-7f;  // 2^-20
     R.mq = e * ((fabsf(R.kq) * (fabsf(R.p1) + (float)np) + fabsf(R.q1)) / dq + nq2 + 2.0f);
     R.mz = e * ((fabsf(R.kz) * (fabsf(R.p1) + (float)np) + fabsf(z1)) / k.dz + k.nz2 + 2.0f);
-    R.pad1 = 0;
+    R.tA = R.tB = 0.0f;
+    if (TOF) {
+        // d(ip) = ((pc(ip) - p1) / pd - ratio1) L with pc = (ip - np/2 + 0.5) dpc, linear in ip
+        const float dpc = xdom ? 1.0f : k.dy;
+        const float ipd = 1.0f / pd;
+        R.tA = dpc * ipd * L;
+        R.tB = (((0.5f - (float)(np / 2)) * dpc - R.p1) * ipd - R.ratio1) * L;
+        R.wc *= k.tof_amp;
+    }
+    proj_slab_range(R.p1, R.p2, xdom, TOF, np2, np, R.pmlo, R.pmhi);
     return R;
 }
 
@@ -160,8 +224,8 @@ __device__ __forceinline__ LorRec setup_rec(const float *l, float tv, float yv, 
 struct LorRun {
     float p1, p2, q1, z1, kq, kz, wc, pd, ratio1, L;
     float np2, nq2, dq, dpc;
-    float Aq, Bq, Az, Bz, inv_pd, mq, mz;
-    int np, nq, nz, np_half, lo, hi;
+    float Aq, Bq, Az, Bz, mq, mz, tA, tB, invq, invz;
+    int np, nq, nz, np_half, lo, hi, pmlo, pmhi;
     int32_t sp, sq, szs;
     bool xdom, dq_one;
 };
@@ -175,7 +239,8 @@ __device__ __forceinline__ LorRun make_run(const LorRec &R, const Grid &g, const
     r.pd = R.pd;
     r.ratio1 = R.ratio1;
     r.L = R.L;
-    r.Aq = R.Aq; r.Bq = R.Bq; r.Az = R.Az; r.Bz = R.Bz; r.inv_pd = R.inv_pd; r.mq = R.mq; r.mz = R.mz;
+    r.Aq = R.Aq; r.Bq = R.Bq; r.Az = R.Az; r.Bz = R.Bz; r.mq = R.mq; r.mz = R.mz;
+    r.tA = R.tA; r.tB = R.tB; r.invq = R.invq; r.invz = R.invz; r.pmlo = R.pmlo; r.pmhi = R.pmhi;
     r.np = r.xdom ? g.nx : g.ny;
     r.nq = r.xdom ? g.ny : g.nx;
     r.nz = g.nz;
@@ -197,12 +262,9 @@ __device__ __forceinline__ LorRun make_run(const LorRec &R, const Grid &g, const
 // Distance of t from the nearest integer is below m (a floor() of t could differ from the floor
 // of a value within m of t).
 __device__ __forceinline__ bool near_int(float t, float m) {
-    const float f = t - floorf(t);
-    return f < m || f > 1.0f - m;
+    return fabsf(t - rintf(t)) < m;
 }
 
-// Relative margin on the TOF truncation test t2 <= nsigma^2 (fast t2 is within ~1e-5 relative).
-constexpr float kTruncMargin = 2e-4f;
 
 // Voxels of one slab from the boundary coordinates: the branch-free form of the reference's case
 // analysis (siddon.cu.cc:86-189). With fq, fz the fractions of the slab before the q and z
@@ -216,8 +278,8 @@ __device__ __forceinline__ void slab_voxels(const LorRun &r, int ip, bool keep, 
     const int cz1 = ifloor(zz1), cz2 = ifloor(zz2);
     const bool dq = cq1 != cq2, dz = cz1 != cz2;
     const bool R = keep && cq1 >= (dq ? -1 : 0) && cq1 < r.nq && cz1 >= (dz ? -1 : 0) && cz1 < r.nz;
-    const float fq = __fdividef((float)cq2 - qq1, qq2 - qq1);  // used only when dq
-    const float fz = __fdividef((float)cz2 - zz1, zz2 - zz1);  // used only when dz
+    const float fq = ((float)cq2 - qq1) * r.invq;  // used only when dq
+    const float fz = ((float)cz2 - zz1) * r.invz;  // used only when dz
     const float f0 = fminf(dq ? fq : 1.0f, dz ? fz : 1.0f);
     const float f2 = 1.0f - fmaxf(dq ? fq : 0.0f, dz ? fz : 0.0f);
     const int32_t base = ip * r.sp;
@@ -235,11 +297,6 @@ __device__ __forceinline__ void slab_voxels(const LorRun &r, int ip, bool keep, 
     w[1] = v1 ? fabsf(fq - fz) * wt : 0.0f;
 }
 
-__device__ __forceinline__ bool proj_slab_rule(const LorRun &r, bool tof, float pp1, float pp2) {
-    if (!tof) return !((r.p1 < r.p2 && pp2 > r.p2) || (r.p1 >= r.p2 && pp1 < r.p2));
-    if (r.xdom) return !((r.p2 > r.p1 && pp1 <= r.p1) || (r.p2 < r.p1 && pp2 >= r.p1));
-    return !((r.p2 > r.p1 && pp1 < r.p1) || (r.p2 < r.p1 && pp2 > r.p1));
-}
 
 // Fast, branch-free candidates of slab ip. `bad` is set when a floor or the truncation test is
 // within its rounding margin; the caller then recomputes the slab with candidates_exact.
@@ -250,18 +307,17 @@ __device__ __forceinline__ void candidates_fast(const LorRun &r, const GridK &k,
     bad = false;
     float w_tof = 1.0f;
     if (TOF) {
-        const float pc = __fmul_rn(__fadd_rn((float)(ip - r.np_half), 0.5f), r.dpc);
-        const float d2 = ((pc - r.p1) * r.inv_pd - r.ratio1) * r.L;
-        const float t2 = d2 * d2 * k.inv_expand;
+        const float d2 = fmaf(r.tA, (float)ip, r.tB);
+        const float e2 = d2 * d2 * k.k2;  // -t2 log2(e) / 2
         if (k.nsig2 > 0.0f) {
-            bad = fabsf(t2 - k.nsig2) <= kTruncMargin * k.nsig2;
-            keep = keep && (t2 <= k.nsig2);
+            bad = fabsf(e2 - k.e2cut) <= k.e2tol;
+            keep = keep && (e2 >= k.e2cut);
         }
-        w_tof = k.tof_amp * exp2f(t2 * -0.72134752044448170f);  // exp(-t2/2)
+        w_tof = exp2f(e2);  // exp(-t2 / 2); the amplitude is in wc
     }
     const float pp1 = __fsub_rn((float)ip, r.np2);
     const float pp2 = __fadd_rn(pp1, 1.0f);
-    pm = proj_slab_rule(r, TOF, pp1, pp2);
+    pm = (ip >= r.pmlo) & (ip <= r.pmhi);
     float qa, qb;
     if (r.dq_one) {  // exact and cheap without a division
         qa = __fadd_rn(__fadd_rn(r.q1, __fmul_rn(r.kq, __fsub_rn(pp1, r.p1))), r.nq2);
@@ -291,11 +347,11 @@ __device__ __forceinline__ void candidates_exact(const LorRun &r, const GridK &k
         const float d2 = __fmul_rn(__fsub_rn(__fdiv_rn(__fsub_rn(pc, r.p1), r.pd), r.ratio1), r.L);
         const float t2 = __fdiv_rn(__fmul_rn(d2, d2), k.expand);
         if (k.nsig2 > 0.0f) keep = t2 <= k.nsig2;
-        w_tof = k.tof_amp * exp2f(t2 * -0.72134752044448170f);
+        w_tof = exp2f(t2 * -kHalfLog2e);  // the amplitude is in wc
     }
     const float pp1 = __fsub_rn((float)ip, r.np2);
     const float pp2 = __fadd_rn(pp1, 1.0f);
-    pm = proj_slab_rule(r, TOF, pp1, pp2);
+    pm = (ip >= r.pmlo) & (ip <= r.pmhi);
     const float qa = bcoord(r.q1, r.kq, pp1, r.p1, r.dq, r.nq2, r.dq_one);
     const float qb = bcoord(r.q1, r.kq, pp2, r.p1, r.dq, r.nq2, r.dq_one);
     const float za = bcoord(r.z1, r.kz, pp1, r.p1, k.dz, k.nz2, false);

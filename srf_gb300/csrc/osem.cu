@@ -351,9 +351,13 @@ __device__ __forceinline__ void decode_study(const srf_study &st, const TofParam
 }
 
 // Persistent kernel over all studies' LOR batches: warp-batch b belongs to the study s with
-// boff[s] <= b < boff[s + 1] (32 LORs per batch, each study padded to whole batches). The batch
-// offsets are staged in shared memory (when they fit), so the lookup costs a few shared-memory
-// reads per batch, and a warp decodes a study descriptor only when it moves to another study.
+// boff[s] <= b < boff[s + 1] (32 LORs per batch, each study padded to whole batches). Warps take
+// batches in order from a ticket counter (work[0]) rather than by a fixed stride, so all warps
+// stay within about one batch per warp of a common frontier: only the one or two studies under
+// the frontier have their images in L2 (with fixed strides the warps drift apart and several
+// studies' images compete for it). The last block to finish returns both counters to zero for
+// the next launch in stream order. The batch offsets are staged in shared memory (when they
+// fit), and a warp decodes a study descriptor only when it moves to another study.
 template <int G, bool TOF, int U, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB)
 k_osem_batch(const srf_study *__restrict__ studies, int n_studies, const int64_t *__restrict__ boff,
@@ -366,15 +370,18 @@ k_osem_batch(const srf_study *__restrict__ studies, int n_studies, const int64_t
         for (int t = threadIdx.x; t <= n_studies; t += blockDim.x) soff[t] = __ldg(boff + t);
     __syncthreads();
     const int64_t *off = staged ? soff : boff;
+    unsigned long long *work = reinterpret_cast<unsigned long long *>(const_cast<int64_t *>(boff + n_studies + 1));
     const int wib = threadIdx.x >> 5;
     const int lane32 = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const bool want_ll = loglik != nullptr;
     WarpStudy &w = wst[wib];
     double ll = 0.0;
     int s = -1;
-    for (int64_t b = warp; b < total_batches; b += nwarps) {
+    for (;;) {
+        unsigned long long ticket = 0;
+        if (lane32 == 0) ticket = atomicAdd(work, 1ULL);
+        const int64_t b = (int64_t)__shfl_sync(0xffffffffu, ticket, 0);
+        if (b >= total_batches) break;
         if (s < 0 || b < off[s] || b >= off[s + 1]) {  // uniform over the warp
             int lo = 0, hi = n_studies;  // off[lo] <= b < off[hi]
             while (hi - lo > 1) {
@@ -395,6 +402,15 @@ k_osem_batch(const srf_study *__restrict__ studies, int n_studies, const int64_t
 #pragma unroll
         for (int o2 = 16; o2 > 0; o2 >>= 1) ll += __shfl_xor_sync(0xffffffffu, ll, o2);
         if (lane32 == 0 && ll != 0.0) atomicAdd(loglik, ll);
+    }
+    __syncthreads();  // every warp of the block has taken its last ticket
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(work + 1, 1ULL) == gridDim.x - 1) {  // last block: reset for the next launch
+            atomicExch(work, 0ULL);
+            atomicExch(work + 1, 0ULL);
+            __threadfence();
+        }
     }
 }
 

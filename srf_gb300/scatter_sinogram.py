@@ -12,8 +12,8 @@ index. For the learned surrogate a 2x-downsampled, regular sinogram is defined h
   opposite crystal, i.e. LORs up to 300 mm from the axis: the whole 600 mm transaxial FOV.
 
 ``sss_sinogram`` fills it with the repository's own single-scatter simulation (srf_sss, with
-the preprocessing projections on the GPU projector); ``features`` are the inputs of the network:
-emission line integrals and attenuation factors along each bin's LOR.
+the preprocessing projections on the GPU projector); ``network_input`` holds the inputs of the
+learned surrogate: emission line integrals and attenuation factors along the bins' LORs.
 """
 from __future__ import annotations
 
@@ -71,6 +71,7 @@ class CoarseGeometry:
         self.bin_lors = torch.as_tensor(lors.astype(np.float32), device=self.device)
         self.ic = ImageConfig(list(VOL_SHAPE), [0.0, 0.0, 0.0], list(FOV_MM))
         self.scatter_points = self._scatter_points()
+        self.coarse_points = self._coarse_points()
 
     def _scatter_points(self) -> np.ndarray:
         """Every floor(50 mm / voxel) voxels, as preprocess.py:6-18 places them."""
@@ -78,6 +79,16 @@ class CoarseGeometry:
         from .data import Image
         img = Image(np.zeros(VOL_SHAPE, np.float32), self.ic.center, self.ic.size)
         return pre_all_scatter_position(img)
+
+    def _coarse_points(self) -> np.ndarray:
+        """The centres of 2 x 2 transaxial groups of the SSS scatter points (all axial layers): a
+        quarter of the points, spread over the same region (input of the learned surrogate)."""
+        p = self.scatter_points
+        xs, ys, zs = (np.unique(p[:, c]) for c in range(3))
+        cx = 0.5 * (xs[0::2][: len(xs) // 2] + xs[1::2][: len(xs) // 2])
+        cy = 0.5 * (ys[0::2][: len(ys) // 2] + ys[1::2][: len(ys) // 2])
+        X, Y, Z = np.meshgrid(cx, cy, zs, indexing="ij")
+        return np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1).astype(np.float32)
 
     def n_bins(self) -> int:
         return self.pairs.shape[0]
@@ -149,13 +160,15 @@ def random_phantom(seed: int, device="cuda") -> Tuple[torch.Tensor, torch.Tensor
 
 def sss_sinogram(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor,
                  low: int = 350, high: int = 650, resolution: float = 0.15,
-                 bins: torch.Tensor = None) -> torch.Tensor:
+                 bins: torch.Tensor = None, points: torch.Tensor = None) -> torch.Tensor:
     """Raw SSS sums of every bin (or of the bins listed) as a flat FP32 tensor.
 
     The preprocessing of preprocess.py (emission line integrals x L^2 and attenuation factors
     from every detector to every scatter point, detector-major) runs on the GPU projector; with
-    ``bins`` only the virtual crystals those bins touch are preprocessed."""
-    sp = torch.as_tensor(geo.scatter_points, dtype=torch.float32, device=geo.device)
+    ``bins`` only the virtual crystals those bins touch are preprocessed. ``points`` replaces the
+    scatter points (default: the reference's every-50-mm grid)."""
+    sp = torch.as_tensor(geo.scatter_points if points is None else points, dtype=torch.float32,
+                         device=geo.device)
     ic = geo.ic
     pairs = geo.pairs_dev if bins is None else geo.pairs_dev.index_select(0, bins)
     if bins is None:
@@ -178,24 +191,15 @@ def sss_sinogram(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor,
     return sc
 
 
-def features(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor) -> torch.Tensor:
-    """(2, n_bins) FP32: emission line integral (projector x L^2) and attenuation factor."""
-    ic = geo.ic
-    Lb = geo.bin_lors
-    p = kernels.project(Lb, kernels.xfast(emission), ic.center, ic.size)
-    len2 = ((Lb[:, 3] - Lb[:, 0]) ** 2 + (Lb[:, 4] - Lb[:, 1]) ** 2 + (Lb[:, 5] - Lb[:, 2]) ** 2)
-    a = kernels.attenuation(Lb, kernels.xfast(mu), ic.center, ic.size)
-    return torch.stack([p * len2, a])
-
-
 # ---------------------------------------------------------------- network grid
-# The network sees the sinogram on a padded (planes, radial, views) = (56, 56, 320) grid: views
-# wrap around (4 copies each side), planes and radial bins repeat their last row. Pooled 2x, the
-# grid is (28, 28, 160), three U-Net levels deep without remainders.
+# The network predicts the sinogram on a padded (planes, radial, views) = (56, 56, 320) grid: views
+# wrap around (4 copies each side), planes and radial bins repeat their last row. It runs on the
+# 2x coarser (28, 28, 160) grid (three U-Net levels without remainders), whose sub-voxel head
+# writes the full grid.
 PAD_GRID = (56, 56, 320)
 VIEW_PAD = 4
 HALF_GRID = (28, 28, 160)
-N_FEATURES = 7
+N_FEATURES = 15
 
 
 def pad_sino(g: torch.Tensor) -> torch.Tensor:
@@ -212,42 +216,90 @@ def crop_sino(t: torch.Tensor) -> torch.Tensor:
     return c.reshape(*t.shape[:-3], -1)
 
 
-def half_mask(device) -> torch.Tensor:
-    """(28, 28, 160) FP32: 1 on half-resolution cells that cover real bins, 0 on pure padding."""
-    m = torch.zeros(HALF_GRID, dtype=torch.float32, device=device)
-    m[: (PLANES - 1 + 1) // 2, : RADIAL // 2, VIEW_PAD // 2: (VIEW_PAD + VIEWS) // 2] = 1.0
+def full_mask(device) -> torch.Tensor:
+    """(56, 56, 320) FP32: 1 on real bins, 0 on padding."""
+    m = torch.zeros(PAD_GRID, dtype=torch.float32, device=device)
+    m[: PLANES - 1, :RADIAL, VIEW_PAD: VIEW_PAD + VIEWS] = 1.0
     return m
 
 
+def _half_cells(geo: CoarseGeometry):
+    """Per half-resolution cell (28 x 28 x 160, flattened): the bin it samples (plane 2z, radial
+    2y, view 2x - 4, clamped/wrapped like the padding), that bin's LOR, and the constant input
+    channels (radial and plane coordinates in [-1, 1], 1 on cells over real bins)."""
+    if getattr(geo, "_half", None) is None:
+        dev = geo.device
+        pz = torch.clamp(torch.arange(HALF_GRID[0], device=dev) * 2, max=PLANES - 2)
+        ry = torch.clamp(torch.arange(HALF_GRID[1], device=dev) * 2, max=RADIAL - 1)
+        vx = (torch.arange(HALF_GRID[2], device=dev) * 2 - VIEW_PAD) % VIEWS
+        idx = ((pz[:, None, None] * RADIAL + ry[None, :, None]) * VIEWS + vx[None, None, :]).reshape(-1)
+        shape = HALF_GRID
+        rc = ((ry.float() - (RADIAL - 1) / 2) / ((RADIAL - 1) / 2))[None, :, None].expand(shape)
+        pc = ((pz.float() - (PLANES - 2) / 2) / ((PLANES - 2) / 2))[:, None, None].expand(shape)
+        real = torch.zeros(shape, device=dev)
+        real[: PLANES // 2, : RADIAL // 2, VIEW_PAD // 2: (VIEW_PAD + VIEWS) // 2] = 1.0
+        const = torch.stack([rc, pc, real], -1).reshape(-1, 3)
+        geo._half = (idx, geo.bin_lors.index_select(0, idx).contiguous(), const)
+    return geo._half
+
+
+def coarse_sss_points(geo: CoarseGeometry, mu: torch.Tensor) -> torch.Tensor:
+    """The coarse scatter points whose nearest voxel has mu > 0 (the others add exactly 0)."""
+    pts = torch.as_tensor(geo.coarse_points, device=mu.device)
+    shape = torch.tensor(mu.shape, device=mu.device)
+    size = torch.tensor(geo.ic.size, dtype=torch.float32, device=mu.device)
+    idx = ((pts / size + 0.5) * shape).long()
+    idx = torch.minimum(torch.clamp(idx, min=0), shape - 1)
+    keep = mu[idx[:, 0], idx[:, 1], idx[:, 2]] > 0
+    return pts[keep].contiguous()
+
+
 def network_input(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor,
-                  feats: torch.Tensor = None) -> Tuple[torch.Tensor, float]:
-    """(1, 56, 56, 320, 16) bfloat16 network input at full resolution and the emission scale.
+                  coarse_scale: float = 1.0) -> Tuple[torch.Tensor, float]:
+    """(1, 28, 28, 160, 16) bfloat16 network input and the emission scale.
 
-    Channels: emission line integral / its mean (e), attenuation factor (a), e * a, the mu line
-    integral / 4, the radial and plane coordinates in [-1, 1], and a constant; 7..15 are zero.
-    Targets and predictions are in units of the emission scale, so the network is scale-free."""
-    f = features(geo, emission, mu) if feats is None else feats
-    e, a = f[0], f[1]
+    Each half-resolution cell samples one bin's LOR. Local channels: emission line integral / its
+    mean over the cells (e), attenuation factor (a), e * a, the mu line integral / 4 (m), and a
+    cheap SSS of the cell's bin over a quarter of the scatter points (coarse_sss_points), in units
+    of the emission scale / coarse_scale. Context channels (scatter at a bin sums over the whole
+    object, more than a 3-level U-Net sees): e, a and e * a averaged over the views of the cell's
+    (plane, radial) row, e and m averaged over its plane, e * a and m averaged over all cells.
+    Geometry channels: the radial and plane coordinates, 1 on cells over real bins. Targets and
+    predictions are in units of the emission scale, so the network is scale-free."""
+    idx, L, const = _half_cells(geo)
+    ic = geo.ic
+    p = kernels.project(L, kernels.xfast(emission), ic.center, ic.size)
+    len2 = ((L[:, 3] - L[:, 0]) ** 2 + (L[:, 4] - L[:, 1]) ** 2 + (L[:, 5] - L[:, 2]) ** 2)
+    e = p * len2
+    a = kernels.attenuation(L, kernels.xfast(mu), ic.center, ic.size)
     scale = float(e.mean().item())
-    en = e / max(scale, 1e-30)
-    P, R, V = PLANES - 1, RADIAL, VIEWS
-    dev = e.device
-    rc = ((torch.arange(R, device=dev, dtype=torch.float32) - (R - 1) / 2) / ((R - 1) / 2))
-    pc = ((torch.arange(P, device=dev, dtype=torch.float32) - (P - 1) / 2) / ((P - 1) / 2))
-    chans = [en, a, en * a, -torch.log(torch.clamp(a, min=1e-30)) * 0.25,
-             rc[None, :, None].expand(P, R, V).reshape(-1), pc[:, None, None].expand(P, R, V).reshape(-1),
-             torch.ones_like(en)]
-    x = torch.stack([c.reshape(P, R, V) for c in chans])          # (7, 51, 52, 312)
-    x = pad_sino(x).permute(1, 2, 3, 0)                               # (56, 56, 320, 7)
-    full = torch.zeros((1, *PAD_GRID, 16), dtype=torch.bfloat16, device=dev)
-    full[0, ..., :N_FEATURES] = x.to(torch.bfloat16)
-    return full, scale
+    pts = coarse_sss_points(geo, mu)
+    if pts.shape[0] > 0:
+        cs = sss_sinogram(geo, emission, mu, bins=idx, points=pts)
+    else:
+        cs = torch.zeros_like(e)
+    cs = (cs / (max(scale, 1e-30) * coarse_scale)).reshape(HALF_GRID)
+    en = (e / max(scale, 1e-30)).reshape(HALF_GRID)
+    a = a.reshape(HALF_GRID)
+    ea = en * a
+    m = -torch.log(torch.clamp(a, min=1e-30)) * 0.25
+    row = lambda t: t.mean(dim=2, keepdim=True).expand(HALF_GRID)
+    plane = lambda t: t.mean(dim=(1, 2), keepdim=True).expand(HALF_GRID)
+    glob = lambda t: t.mean().expand(HALF_GRID)
+    feats = [en, a, ea, m, cs, row(en), row(a), row(ea), plane(en), plane(m), glob(ea), glob(m)]
+    x = torch.empty((*HALF_GRID, 16), dtype=torch.bfloat16, device=L.device)
+    x[..., :len(feats)] = torch.stack(feats, -1).to(torch.bfloat16)
+    x[..., len(feats):len(feats) + 3] = const.reshape(*HALF_GRID, 3).to(torch.bfloat16)
+    x[..., len(feats) + 3:] = 0
+    return x.reshape(1, *HALF_GRID, 16), scale
 
 
-def target_half(sino_flat: torch.Tensor, scale: float) -> torch.Tensor:
-    """(28, 28, 160) FP32 training target: the scatter sinogram / scale, padded and 2x pooled."""
-    g = pad_sino((sino_flat / scale).reshape(PLANES - 1, RADIAL, VIEWS))
-    return torch.nn.functional.avg_pool3d(g[None, None], 2)[0, 0].contiguous()
+COARSE_CHANNEL = 4
+
+
+def target_full(sino_flat: torch.Tensor, scale: float) -> torch.Tensor:
+    """(56, 56, 320) FP32 training target: the scatter sinogram / scale on the padded grid."""
+    return pad_sino((sino_flat / scale).reshape(PLANES - 1, RADIAL, VIEWS)).contiguous()
 
 
 # ---------------------------------------------------------------- synthetic scatter events

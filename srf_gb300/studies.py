@@ -91,7 +91,8 @@ class StudyBatch:
                 d.size[:] = st.size
                 off.append(off[-1] + (per + 31) // 32)
             self.desc.append(_to_device_bytes(arr, dev))
-            self.boff.append(torch.as_tensor(off, dtype=torch.int64, device=dev))
+            # two zeroed work counters follow the offsets (the batch kernel's batch tickets)
+            self.boff.append(torch.as_tensor(off + [0, 0], dtype=torch.int64, device=dev))
             self.total.append(off[-1])
         toff = [0]
         for st in studies:

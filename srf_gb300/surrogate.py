@@ -12,9 +12,10 @@ Architecture on a (D, H, W) grid (the half-resolution sinogram), channels (32, 6
     pool -> e3a, e3b: 64->96->96
     up + skip(e2b) -> d2a, d2b: 160->64->64
     up + skip(e1b) -> d1a, d1b: 96->32->32
-    1x1x1 head: 32->1 (FP32)
+    sub-voxel 1x1x1 head: 32->8 FP32 outputs per voxel, one per voxel of the 2x finer grid
 ReLU after every 3x3x3 convolution. Skip concatenation is free: e1b/e2b write straight into the
-channel slices the decoder reads.
+channel slices the decoder reads. The network runs on the 2x-pooled sinogram and its head writes
+the full-resolution sinogram directly (no interpolation floor).
 
 ``ScatterSurrogate`` wraps the network with SSS as the judge: ``estimate`` predicts the scatter
 sinogram and, when a spot-check SSS on a subset of bins differs by more than ``fallback_tol``
@@ -77,8 +78,8 @@ class UNet3D:
         self.e3a, self.e3b = Conv3(c2, c3, g, self.device), Conv3(c3, c3, g, self.device)
         self.d2a, self.d2b = Conv3(c3 + c2, c2, g, self.device), Conv3(c2, c2, g, self.device)
         self.d1a, self.d1b = Conv3(c2 + c1, c1, g, self.device), Conv3(c1, c1, g, self.device)
-        self.hw = (torch.randn(c1, generator=g) * math.sqrt(1.0 / c1)).to(self.device)
-        self.hb = torch.zeros(1, device=self.device)
+        self.hw = (torch.randn(8, c1, generator=g) * math.sqrt(1.0 / c1)).to(self.device)
+        self.hb = torch.zeros(8, device=self.device)
         self.ghw = torch.zeros_like(self.hw)
         self.ghb = torch.zeros_like(self.hb)
         self.convs = [self.e1a, self.e1b, self.e2a, self.e2b, self.e3a, self.e3b, self.d2a,
@@ -92,7 +93,7 @@ class UNet3D:
             c.refresh(s)
 
     def n_params(self) -> int:
-        return sum(c.w.numel() + c.b.numel() for c in self.convs) + self.hw.numel() + 1
+        return sum(c.w.numel() + c.b.numel() for c in self.convs) + self.hw.numel() + self.hb.numel()
 
     def _alloc(self, n: int, g1):
         if self.shape == (n, tuple(g1)):
@@ -110,7 +111,7 @@ class UNet3D:
         b["e3a"], b["e3b"] = z(g3, c3), z(g3, c3)
         b["d2a"], b["d2b"] = z(g2, c2), z(g2, c2)
         b["d1a"], b["d1b"] = z(g1, c1), z(g1, c1)
-        b["out"] = torch.zeros((n, *g1), dtype=F32, device=dev)
+        b["out"] = torch.zeros((n, *(2 * s for s in g1)), dtype=F32, device=dev)
         for k in ("d1b", "d1a", "cat1", "d2b", "d2a", "cat2", "e3b", "e3a", "l3in", "e2a", "l2in", "e1a"):
             b["g_" + k] = torch.zeros_like(b[k])
         b["g_pool2"] = z(g2, c2)
@@ -123,8 +124,11 @@ class UNet3D:
         call("srf_conv3d_fwd", ptr(x), act(x, xoff), i32(layer.cin), ptr(layer.wb), ptr(layer.b),
              i32(layer.cout), i32(1 if relu else 0), ptr(y), act(y, yoff), None, s)
 
+    def _fine(self):
+        return (ctypes.c_int32 * 3)(*self.buf["out"].shape[1:])
+
     def forward(self, inp: torch.Tensor) -> torch.Tensor:
-        """inp: (N, D, H, W, 16) bfloat16 -> (N, D, H, W) float32."""
+        """inp: (N, D, H, W, 16) bfloat16 -> (N, 2D, 2H, 2W) float32."""
         n, d, h, w, c = inp.shape
         assert c == self.IN_CH and inp.dtype == BF16
         self._alloc(n, (d, h, w))
@@ -145,8 +149,8 @@ class UNet3D:
         call("srf_cnn_upsample2", ptr(b["d2b"]), act(b["d2b"]), ptr(b["cat1"]), act(b["cat1"], 0), i32(c2), i32(0), s)
         self._conv(self.d1a, b["cat1"], 0, b["d1a"], 0, s=s)
         self._conv(self.d1b, b["d1a"], 0, b["d1b"], 0, s=s)
-        call("srf_cnn_head", ptr(b["d1b"]), act(b["d1b"]), i32(c1), ptr(self.hw), ptr(self.hb),
-             ptr(b["out"]), None, None, None, None, None, s)
+        call("srf_cnn_head8", ptr(b["d1b"]), act(b["d1b"]), i32(c1), ptr(self.hw), ptr(self.hb),
+             ptr(b["out"]), self._fine(), None, None, None, None, None, s)
         return b["out"]
 
     # ---------------------------------------------------------------- backward
@@ -161,11 +165,12 @@ class UNet3D:
                  i32(layer.cin), i32(0), ptr(gx), act(gx, gxoff), None, s)
 
     def backward(self, gout: torch.Tensor) -> None:
-        """Accumulate parameter gradients for d(loss)/d(out) = gout (N, D, H, W) float32."""
+        """Accumulate parameter gradients for d(loss)/d(out) = gout (N, 2D, 2H, 2W) float32."""
         b, s = self.buf, stream_ptr(self.device)
         c1, c2, c3 = self.c
-        call("srf_cnn_head", ptr(b["d1b"]), act(b["d1b"]), i32(c1), ptr(self.hw), ptr(self.hb), None,
-             ptr(gout.contiguous()), ptr(b["g_d1b"]), act(b["g_d1b"]), ptr(self.ghw), ptr(self.ghb), s)
+        call("srf_cnn_head8", ptr(b["d1b"]), act(b["d1b"]), i32(c1), ptr(self.hw), ptr(self.hb), None,
+             self._fine(), ptr(gout.contiguous()), ptr(b["g_d1b"]), act(b["g_d1b"]), ptr(self.ghw),
+             ptr(self.ghb), s)
         self._conv_bwd(self.d1b, b["d1a"], 0, b["d1b"], 0, b["g_d1b"], 0, b["g_d1a"], 0, s)
         self._conv_bwd(self.d1a, b["cat1"], 0, b["d1a"], 0, b["g_d1a"], 0, b["g_cat1"], 0, s)
         call("srf_cnn_upsample2", ptr(b["g_d2b"]), act(b["g_d2b"]), ptr(b["g_cat1"]), act(b["g_cat1"], 0), i32(c2), i32(1), s)
@@ -222,25 +227,6 @@ class UNet3D:
         return out
 
 
-def upsample_trilinear2(x: torch.Tensor, out_shape) -> torch.Tensor:
-    """(N, d, h, w) float32 -> (N, D, H, W) by trilinear 2x interpolation (srf_cnn_trilinear2)."""
-    n, d, h, w = x.shape
-    D, H, W = out_shape
-    out = torch.empty((n, D, H, W), dtype=F32, device=x.device)
-    call("srf_cnn_trilinear2", ptr(x.contiguous()), i32(n), i32(d), i32(h), i32(w), ptr(out), i32(D),
-         i32(H), i32(W), stream_ptr(x.device))
-    return out
-
-
-def pool_input(full: torch.Tensor) -> torch.Tensor:
-    """(N, D, H, W, 16) bfloat16 at full resolution -> half resolution (srf_cnn_pool2)."""
-    n, d, h, w, c = full.shape
-    g = half((d, h, w))
-    out = torch.empty((n, *g, c), dtype=BF16, device=full.device)
-    call("srf_cnn_pool2", ptr(full), act(full), ptr(out), act(out), i32(c), i32(0), stream_ptr(full.device))
-    return out
-
-
 # ---------------------------------------------------------------- weights
 def save_weights(net: UNet3D, path: str, meta: Dict[str, float]) -> None:
     """FP32 master weights and metadata (numpy .npz, no pickled objects)."""
@@ -288,27 +274,39 @@ class ScatterSurrogate:
     on ``spot_bins`` random bins, and whether that exceeded ``fallback_tol`` so that the full SSS
     was returned instead."""
 
-    def __init__(self, geo, net: UNet3D, target_scale: float, fallback_tol: float = 0.05,
-                 spot_bins: int = 2048, seed: int = 0):
-        self.geo, self.net, self.k = geo, net, float(target_scale)
+    def __init__(self, geo, net: UNet3D, target_scale: float, coarse_scale: float = 1.0,
+                 fallback_tol: float = 0.05, spot_bins: int = 2048, seed: int = 0):
+        self.geo, self.net, self.k, self.kc = geo, net, float(target_scale), float(coarse_scale)
         self.fallback_tol, self.spot_bins = fallback_tol, spot_bins
         self.gen = torch.Generator(device=geo.device).manual_seed(seed)
 
     @classmethod
     def load(cls, geo, path: str = DEFAULT_WEIGHTS, **kw) -> "ScatterSurrogate":
         net, meta = load_weights(path, geo.device)
-        return cls(geo, net, meta["target_scale"], **kw)
+        return cls(geo, net, meta["target_scale"], meta.get("coarse_scale", 1.0), **kw)
 
     def predict(self, emission: torch.Tensor, mu: torch.Tensor) -> torch.Tensor:
-        from .scatter_sinogram import PAD_GRID, crop_sino, network_input
-        full, scale = network_input(self.geo, emission, mu)
-        out = self.net.forward(pool_input(full))                       # (1, 28, 28, 160)
-        up = upsample_trilinear2(out, PAD_GRID)                          # (1, 56, 56, 320)
-        return crop_sino(up)[0] * (self.k * scale)
+        from .scatter_sinogram import crop_sino, network_input
+        inp, scale = network_input(self.geo, emission, mu, self.kc)
+        out = self.net.forward(inp)                                     # (1, 56, 56, 320)
+        return crop_sino(out)[0] * (self.k * scale)
+
+    def draw_spot_bins(self) -> torch.Tensor:
+        """``spot_bins`` random bins whose virtual crystals lie in a random pool of 48 of the 312
+        transaxial positions (all rings): the spot-check SSS then preprocesses 1,248 crystals
+        instead of 8,112 while the bins still spread over every plane, radius and 48 views."""
+        geo = self.geo
+        pos = torch.randperm(geo.vt, generator=self.gen, device=geo.device)[:48]
+        pool = torch.zeros(geo.vt * geo.vr, dtype=torch.bool, device=geo.device)
+        pool[(torch.arange(geo.vr, device=geo.device)[:, None] * geo.vt + pos[None, :]).reshape(-1)] = True
+        pr = geo.pairs_dev.long()
+        cand = torch.nonzero(pool[pr[:, 0]] & pool[pr[:, 1]]).reshape(-1)
+        pick = torch.randperm(cand.numel(), generator=self.gen, device=geo.device)[: self.spot_bins]
+        return cand.index_select(0, pick)
 
     def spot_check(self, emission: torch.Tensor, mu: torch.Tensor, pred: torch.Tensor) -> float:
         from .scatter_sinogram import sss_sinogram
-        bins = torch.randperm(self.geo.n_bins(), generator=self.gen, device=self.geo.device)[: self.spot_bins]
+        bins = self.draw_spot_bins()
         ref = sss_sinogram(self.geo, emission, mu, bins=bins)
         p = pred.index_select(0, bins)
         return float((torch.linalg.vector_norm(p - ref) / torch.linalg.vector_norm(ref).clamp_min(1e-30)).item())
@@ -323,32 +321,31 @@ class ScatterSurrogate:
 
 
 # ---------------------------------------------------------------- training
-def build_dataset(geo, seeds, log=None):
-    """Network inputs (N, 28, 28, 160, 16) bf16, targets (N, 28, 28, 160) FP32 in units of each
-    study's emission scale, the scales, and the full-resolution SSS sinograms (N, n_bins)."""
-    from .scatter_sinogram import HALF_GRID, features, network_input, random_phantom, sss_sinogram, target_half
+def build_dataset(geo, seeds, log=None, coarse_scale: float = 1.0):
+    """Network inputs (N, 28, 28, 160, 16) bf16, targets (N, 56, 56, 320) FP32 in units of each
+    study's emission scale, and the scales."""
+    from .scatter_sinogram import HALF_GRID, PAD_GRID, network_input, random_phantom, sss_sinogram, target_full
     n = len(seeds)
     dev = geo.device
     X = torch.empty((n, *HALF_GRID, UNet3D.IN_CH), dtype=BF16, device=dev)
-    T = torch.empty((n, *HALF_GRID), dtype=F32, device=dev)
-    S = torch.empty((n, geo.n_bins()), dtype=F32, device=dev)
+    T = torch.empty((n, *PAD_GRID), dtype=F32, device=dev)
     scales = torch.empty(n, dtype=torch.float64)
     for i, sd in enumerate(seeds):
         em, mu = random_phantom(int(sd), device=dev)
         sc = sss_sinogram(geo, em, mu)
-        full, scale = network_input(geo, em, mu, features(geo, em, mu))
-        X[i] = pool_input(full)[0]
-        T[i] = target_half(sc, scale)
-        S[i] = sc
+        inp, scale = network_input(geo, em, mu, coarse_scale)
+        X[i] = inp[0]
+        T[i] = target_full(sc, scale)
         scales[i] = scale
         if log and (i + 1) % 200 == 0:
             log(f"dataset {i + 1}/{n}")
-    return X, T, scales, S
+    return X, T, scales
 
 
 def train(net: UNet3D, X: torch.Tensor, T: torch.Tensor, mask: torch.Tensor, epochs: int,
-          batch: int = 4, lr: float = 2e-3, seed: int = 0, log=None) -> List[float]:
-    """Adam on the masked relative squared error, cosine-decayed learning rate."""
+          batch: int = 4, lr: float = 2e-3, seed: int = 0, log=None, every=None) -> List[float]:
+    """Adam on the masked relative squared error, cosine-decayed learning rate; ``every(epoch)``
+    runs after each epoch (monitoring)."""
     n = X.shape[0]
     g = torch.Generator().manual_seed(seed)
     inv_den = 1.0 / (T * T * mask).sum(dim=(1, 2, 3)).clamp_min(1e-30)
@@ -372,6 +369,8 @@ def train(net: UNet3D, X: torch.Tensor, T: torch.Tensor, mask: torch.Tensor, epo
                                    inv_den[:batch].contiguous(), None).item()))
         if log:
             log(f"epoch {ep + 1}/{epochs} loss(first batch) {hist[-1]:.5f}")
+        if every:
+            every(ep + 1)
     return hist
 
 
@@ -393,7 +392,7 @@ def main(argv=None) -> None:
     import json
     import time
     from . import synth
-    from .scatter_sinogram import CoarseGeometry, half_mask
+    from .scatter_sinogram import COARSE_CHANNEL, CoarseGeometry, full_mask
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--train", type=int, default=2000)
@@ -407,22 +406,32 @@ def main(argv=None) -> None:
     dev = torch.device("cuda", 0)
     geo = CoarseGeometry(synth.scanner_clinical(), device=dev)
     t0 = time.time()
-    X, T, scales, _ = build_dataset(geo, range(a.train), log)
+    X, T, scales = build_dataset(geo, range(a.train), log)
     torch.cuda.synchronize()
     log(f"dataset built in {time.time() - t0:.1f} s")
-    mask = half_mask(dev)
+    mask = full_mask(dev)
     k = float(((T * mask).sum() / (mask.sum() * T.shape[0])).item())
     T /= k
+    # the coarse-SSS input channel in units of its own dataset mean
+    kc = float(X[..., COARSE_CHANNEL].float().mean().item())
+    X[..., COARSE_CHANNEL] = (X[..., COARSE_CHANNEL].float() / kc).to(BF16)
     net = UNet3D(channels=tuple(int(c) for c in a.channels.split(",")), seed=1, device=dev)
     log(f"parameters {net.n_params()}")
+    sur = ScatterSurrogate(geo, net, k, kc)
+    mon = range(1_000_000, 1_000_000 + 10)
+
+    def every(ep):
+        if ep % 5 == 0 or ep == a.epochs:
+            e = evaluate(sur, mon)
+            log(f"epoch {ep}: held-out rel L2 mean {sum(e) / len(e):.4f} max {max(e):.4f}")
+
     t0 = time.time()
-    hist = train(net, X, T, mask, a.epochs, a.batch, a.lr, log=log)
+    hist = train(net, X, T, mask, a.epochs, a.batch, a.lr, log=log, every=every)
     torch.cuda.synchronize()
     t_train = time.time() - t0
     del X, T
-    sur = ScatterSurrogate(geo, net, k)
     errs = evaluate(sur, range(1_000_000, 1_000_000 + a.held_out))
-    meta = {"target_scale": k, "train_studies": a.train, "epochs": a.epochs, "train_s": t_train,
+    meta = {"target_scale": k, "coarse_scale": kc, "train_studies": a.train, "epochs": a.epochs, "train_s": t_train,
             "held_out_mean_rel_l2": sum(errs) / len(errs), "held_out_max_rel_l2": max(errs)}
     save_weights(net, a.out, meta)
     print(json.dumps({**meta, "loss_history": hist}))

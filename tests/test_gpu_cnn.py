@@ -90,6 +90,37 @@ def test_pool_upsample_and_adjoints(cuda_lib, cnn):
     assert np.allclose(_np(gc), cnn.upsample2_adjoint(_np(x), coarse), atol=1e-2)
 
 
+def test_head8_forward_and_gradients(cuda_lib, cnn):
+    from srf_gb300._lib import call, i32, ptr, stream_ptr
+    from srf_gb300.surrogate import act
+    import ctypes
+    rng = np.random.default_rng(4)
+    dev = torch.device("cuda", 0)
+    n, d, h, w, c = 2, 3, 4, 5, 32
+    fine = (6, 7, 10)  # cropped in y
+    x = _bf(rng.standard_normal((n, d, h, w, c + 8))).to(dev)
+    wt = torch.as_tensor(rng.standard_normal((8, c)).astype(np.float32)).to(dev)
+    b = torch.as_tensor(rng.standard_normal(8).astype(np.float32)).to(dev)
+    out = torch.zeros((n, *fine), dtype=torch.float32, device=dev)
+    f3 = (ctypes.c_int32 * 3)(*fine)
+    s = stream_ptr(dev)
+    call("srf_cnn_head8", ptr(x), act(x, 8), i32(c), ptr(wt), ptr(b), ptr(out), f3, None, None, None,
+         None, None, s)
+    x64 = _np(x)[..., 8:]
+    ref = cnn.head8(x64, wt.cpu().numpy(), b.cpu().numpy(), fine)
+    assert rel_l2(out.cpu().numpy(), ref) <= 1e-5
+    gout = torch.as_tensor(rng.standard_normal((n, *fine)).astype(np.float32)).to(dev)
+    gx = torch.zeros((n, d, h, w, c), dtype=torch.bfloat16, device=dev)
+    gw = torch.zeros((8, c), dtype=torch.float32, device=dev)
+    gb = torch.zeros(8, dtype=torch.float32, device=dev)
+    call("srf_cnn_head8", ptr(x), act(x, 8), i32(c), ptr(wt), ptr(b), None, f3, ptr(gout), ptr(gx),
+         act(gx), ptr(gw), ptr(gb), s)
+    rgx, rgw, rgb = cnn.head8_grads(x64, wt.cpu().numpy(), gout.cpu().numpy().astype(np.float64))
+    assert rel_l2(gw.cpu().numpy(), rgw) <= 1e-5
+    assert rel_l2(gb.cpu().numpy(), rgb) <= 1e-5
+    assert rel_l2(_np(gx), rgx) <= 4e-3
+
+
 def test_unet_gradient_matches_finite_differences_and_trains(cuda_lib):
     """Backpropagated gradients of the whole network against central differences of its own
     forward pass (FP32 head output), and a few Adam steps lowering the loss."""
@@ -101,7 +132,7 @@ def test_unet_gradient_matches_finite_differences_and_trains(cuda_lib):
     inp = np.zeros((n, *g, 16), np.float32)
     inp[..., :2] = rng.random((n, *g, 2))
     inp = _bf(inp).to(dev)
-    target = torch.as_tensor(rng.random((n, *g)).astype(np.float32), device=dev)
+    target = torch.as_tensor(rng.random((n, *(2 * v for v in g))).astype(np.float32), device=dev)
     inv_den = (1.0 / (target ** 2).sum(dim=(1, 2, 3))).contiguous()
 
     def loss_only():
@@ -113,8 +144,8 @@ def test_unet_gradient_matches_finite_differences_and_trains(cuda_lib):
     l0 = float(net.loss(out, target, None, inv_den, grad).item())
     net.zero_grad()
     net.backward(grad)
-    # the head bias: exact linear response, gradient = sum of the output gradient
-    gb = float(net.ghb.item())
+    # the head biases: exact linear response, gradient = sum of the output gradient
+    gb = float(net.ghb.sum().item())
     h = 1e-2
     net.hb += h
     lp = loss_only()
