@@ -122,6 +122,26 @@ int srf_projection_adjoint(const float *lors, int64_t n, int32_t lor_stride,
                            const int32_t grid[3], const float center[3], const float size[3],
                            void *stream);
 
+/* srf_projection / srf_projection_tof and srf_projection_adjoint for n_images (1..8) images that
+ * share one grid and one set of LORs (no counterpart in the reference: the batched forward and
+ * gradient of the differentiable projector). Image b starts batch_stride elements after image b-1
+ * in each layout given (images and the optional images_t); LOR values / outputs are n_images rows
+ * of n at row stride out_stride / values_stride. tof == NULL selects the non-TOF projector. Each
+ * LOR is set up and traversed once for all images. */
+int srf_projection_batch(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
+                         int32_t tof_stride, float tof_bin, float tof_sigma2, float tof_nsigma,
+                         int32_t n_images, int64_t batch_stride, const float *images,
+                         const int64_t image_strides[3], const float *images_t,
+                         const int64_t image_t_strides[3], const int32_t grid[3],
+                         const float center[3], const float size[3], float *out, int64_t out_stride,
+                         void *stream);
+int srf_projection_adjoint_batch(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
+                                 int32_t tof_stride, float tof_bin, float tof_sigma2, float tof_nsigma,
+                                 int32_t n_images, const float *values, int64_t values_stride,
+                                 float *images, int64_t batch_stride, const int64_t image_strides[3],
+                                 float *images_t, const int64_t image_t_strides[3], const int32_t grid[3],
+                                 const float center[3], const float size[3], void *stream);
+
 /* *count += number of (LOR, voxel) weight visits the projector (rules 0) or backprojector
  * (rules 1) rule set makes for these LORs (tof == NULL: non-TOF rules). `count` is a device
  * unsigned 64-bit counter. These are the "LOR-voxel updates" of the throughput metric; the CPU

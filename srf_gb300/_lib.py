@@ -25,7 +25,7 @@ SRF_RATIO_PLAIN = 1
 EXPORTS = (
     "srf_last_error", "srf_version", "srf_set_group_lanes", "srf_set_tuning", "srf_projection", "srf_backprojection",
     "srf_projection_tof", "srf_backprojection_tof", "srf_projection_adjoint", "srf_fold_views",
-    "srf_copy_view", "srf_count_pairs", "srf_osem_subset", "srf_osem_update", "srf_osem_subset_batch",
+    "srf_copy_view", "srf_count_pairs", "srf_projection_batch", "srf_projection_adjoint_batch", "srf_osem_subset", "srf_osem_update", "srf_osem_subset_batch",
     "srf_osem_update_batch", "srf_emap_block_full", "srf_sss",
     "srf_backprojection_tof_noalloc", "srf_listmode_snap", "srf_lm2sino", "srf_attenuation",
     "srf_conv3d_fwd", "srf_conv3d_wgrad", "srf_conv3d_flip_weights", "srf_cnn_relu_bwd",

@@ -7,7 +7,8 @@ projector (projector skip rules and 1/L^2 weights). The reference's backprojecto
 adjoint (no endpoint/steep skips, no 1/L^2), so it cannot serve as a gradient.
 
 ``image`` is (nx, ny, nz) or a batch (B, nx, ny, nz) of float32 CUDA tensors; the result is (N,)
-or (B, N). ``poisson_nll(p, y)`` is the list-mode/binned Poisson negative log-likelihood
+or (B, N). A batch runs through srf_projection_batch / srf_projection_adjoint_batch, which set up
+and traverse each LOR once for up to 8 images. ``poisson_nll(p, y)`` is the list-mode/binned Poisson negative log-likelihood
 sum(p - y log p) used as the training loss.
 """
 from __future__ import annotations
@@ -26,8 +27,9 @@ class _Project(torch.autograd.Function):
         ctx.meta = (list(image.shape[-3:]), list(center), list(size), tof, tof_nsigma, image.dim())
         if image.dim() == 3:
             return kernels.project(lors, image.detach(), center, size, tof=tof, tof_nsigma=tof_nsigma)
-        return torch.stack([kernels.project(lors, im.detach(), center, size, tof=tof,
-                                            tof_nsigma=tof_nsigma) for im in image])
+        B = kernels.MAX_BATCH
+        return torch.cat([kernels.project_batch(lors, image[k:k + B].detach(), center, size, tof=tof,
+                                                tof_nsigma=tof_nsigma) for k in range(0, image.shape[0], B)])
 
     @staticmethod
     def backward(ctx, grad_p: torch.Tensor):
@@ -35,10 +37,13 @@ class _Project(torch.autograd.Function):
         shape, center, size, tof, tof_nsigma, dim = ctx.meta
         g = grad_p.detach().to(torch.float32)
 
-        def adj(v):
-            return kernels.backproject(lors, v.contiguous(), shape, center, size, tof=tof,
+        if dim == 3:
+            grad = kernels.backproject(lors, g.contiguous(), shape, center, size, tof=tof,
                                        tof_nsigma=tof_nsigma, adjoint=True)
-        grad = adj(g) if dim == 3 else torch.stack([adj(v) for v in g])
+        else:
+            B = kernels.MAX_BATCH
+            grad = torch.cat([kernels.adjoint_batch(lors, g[k:k + B], shape, center, size, tof=tof,
+                                                    tof_nsigma=tof_nsigma) for k in range(0, g.shape[0], B)])
         return grad, None, None, None, None, None
 
 

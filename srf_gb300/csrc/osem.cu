@@ -100,7 +100,7 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
         const int j = j0 + gi;
         const LorRec R = load_rec(&wrecs[j]);
         const int64_t i = base + j;
-        if (R.flags & F_TIE) {
+        if (!TOF && (R.flags & F_TIE)) {  // ties exist only under the non-TOF projector rule
             float lv[6];
             const float *l = lors + i * stride;
 #pragma unroll

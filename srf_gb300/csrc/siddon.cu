@@ -92,6 +92,95 @@ static int launch_trace(const float *lors, int64_t n, int stride, const float *t
     }
 }
 
+// Projector and its exact adjoint for a batch of nb <= kMaxBatch images sharing one grid and one
+// set of LORs (image b at offset b * bstride): every LOR is set up and traversed once, and each
+// visit gathers from (or scatters into) all images. out / values hold nb rows of n at row stride
+// ostride.
+constexpr int kMaxBatch = 8;
+
+template <int G, bool TOF, int ACTION>
+__global__ void __launch_bounds__(kBlock)
+k_trace_batch(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
+              int tof_stride, Grid g, TofParams tp, View v, View vt, int nb, int64_t bstride,
+              const float *__restrict__ values, float *__restrict__ out, int64_t ostride) {
+    constexpr int GPW = 32 / G;
+    const int lane = threadIdx.x & (G - 1);
+    const int gi = (threadIdx.x & 31) / G;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool have_t = vt.ptr != nullptr;
+    for (int64_t base = warp * GPW; base < n; base += nwarps * GPW) {
+        const int64_t i = base + gi;
+        const bool valid = i < n;
+        float acc[kMaxBatch];
+#pragma unroll
+        for (int b = 0; b < kMaxBatch; ++b) acc[b] = 0.0f;
+        if (valid) {
+            const float *l = lors + i * stride;
+            const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
+            LorSetup S;
+            if (setup_lor<TOF, RULES_PROJ>(__ldg(l), __ldg(l + 1), __ldg(l + 2), __ldg(l + 3),
+                                           __ldg(l + 4), __ldg(l + 5), tv, g, tp, v.st, vt.st, have_t, S)) {
+                float *im = (!S.xdom && have_t) ? vt.ptr : v.ptr;
+                if (ACTION == GATHER) {
+                    const float *imc = im;
+                    for (int ip = S.lo + lane; ip <= S.hi; ip += G)
+                        slab<TOF, RULES_PROJ>(S, ip, [&](int32_t off, float w) {
+#pragma unroll
+                            for (int b = 0; b < kMaxBatch; ++b)
+                                if (b < nb) acc[b] = fmaf(__ldg(imc + b * bstride + off), w, acc[b]);
+                        });
+                } else {
+                    float val[kMaxBatch];
+                    bool any = false;
+#pragma unroll
+                    for (int b = 0; b < kMaxBatch; ++b) {
+                        val[b] = b < nb ? __ldg(values + b * ostride + i) : 0.0f;
+                        any = any || val[b] != 0.0f;
+                    }
+                    if (any)
+                        for (int ip = S.lo + lane; ip <= S.hi; ip += G)
+                            slab<TOF, RULES_PROJ>(S, ip, [&](int32_t off, float w) {
+#pragma unroll
+                                for (int b = 0; b < kMaxBatch; ++b)
+                                    if (b < nb && val[b] != 0.0f) atomicAdd(im + b * bstride + off, val[b] * w);
+                            });
+                }
+            }
+        }
+        if (ACTION == GATHER) {
+#pragma unroll
+            for (int b = 0; b < kMaxBatch; ++b) {
+                const float r = group_sum<G>(acc[b]);
+                if (valid && lane == 0 && b < nb) out[b * ostride + i] = r;
+            }
+        }
+    }
+}
+
+template <int G, bool TOF, int ACTION>
+static int launch_batch_trace_g(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                                const Grid &g, const TofParams &tp, const View &v, const View &vt, int nb,
+                                int64_t bstride, const float *values, float *out, int64_t ostride,
+                                cudaStream_t s) {
+    auto kern = k_trace_batch<G, TOF, ACTION>;
+    unsigned blocks = grid_for(kern, n, kBlock / G);
+    kern<<<blocks, kBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride);
+    return check_cuda("batched trace kernel launch");
+}
+
+template <bool TOF, int ACTION>
+static int launch_batch_trace(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                              const Grid &g, const TofParams &tp, const View &v, const View &vt, int nb,
+                              int64_t bstride, const float *values, float *out, int64_t ostride, cudaStream_t s) {
+    if (n == 0) return ok();
+    switch (group_lanes()) {
+    case 8: return launch_batch_trace_g<8, TOF, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride, s);
+    case 16: return launch_batch_trace_g<16, TOF, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride, s);
+    default: return launch_batch_trace_g<32, TOF, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride, s);
+    }
+}
+
 // Elementwise kernels over a grid with arbitrary views.
 __global__ void k_fold(float *dst, View d, const float *src, View sv, int nx, int ny, int nz) {
     const int64_t total = (int64_t)nx * ny * nz;
@@ -210,6 +299,60 @@ int srf_projection_adjoint(const float *lors, int64_t n, int32_t lor_stride, con
     }
     TofParams tp{0, 0, 0};
     return launch_trace<false, RULES_PROJ, SCATTER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
+}
+
+static int batch_args(int32_t n_images, int64_t batch_stride, int64_t row_stride, int64_t n,
+                      const View &v, const View &vt, const Grid &g) {
+    if (n_images < 1 || n_images > kMaxBatch) return fail(SRF_EINVAL, "n_images must be 1..%d", kMaxBatch);
+    if (row_stride < n) return fail(SRF_EINVAL, "row stride of the LOR values is below n");
+    int64_t span = 0;  // largest element offset within one image (either layout)
+    for (int k = 0; k < 3; ++k) {
+        const int nk = k == 0 ? g.nx : (k == 1 ? g.ny : g.nz);
+        span += (nk - 1) * (v.st[k] > vt.st[k] ? v.st[k] : vt.st[k]);
+    }
+    if (n_images > 1 && batch_stride <= span) return fail(SRF_EGRID, "images of the batch overlap");
+    return SRF_OK;
+}
+
+int srf_projection_batch(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
+                         int32_t tof_stride, float tof_bin, float tof_sigma2, float tof_nsigma,
+                         int32_t n_images, int64_t batch_stride, const float *images,
+                         const int64_t image_strides[3], const float *images_t,
+                         const int64_t image_t_strides[3], const int32_t grid[3],
+                         const float center[3], const float size[3], float *out, int64_t out_stride,
+                         void *stream) {
+    Grid g; View v, vt; int rc;
+    if ((rc = common_args(lors, n, lor_stride, images, image_strides, images_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
+    if ((rc = batch_args(n_images, batch_stride, out_stride, n, v, vt, g))) return rc;
+    if (n > 0 && !out) return fail(SRF_EINVAL, "out must not be NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (tof) {
+        TofParams tp;
+        if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
+        return launch_batch_trace<true, GATHER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, n_images, batch_stride, nullptr, out, out_stride, s);
+    }
+    TofParams tp{0, 0, 0};
+    return launch_batch_trace<false, GATHER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, n_images, batch_stride, nullptr, out, out_stride, s);
+}
+
+int srf_projection_adjoint_batch(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
+                                 int32_t tof_stride, float tof_bin, float tof_sigma2, float tof_nsigma,
+                                 int32_t n_images, const float *values, int64_t values_stride,
+                                 float *images, int64_t batch_stride, const int64_t image_strides[3],
+                                 float *images_t, const int64_t image_t_strides[3], const int32_t grid[3],
+                                 const float center[3], const float size[3], void *stream) {
+    Grid g; View v, vt; int rc;
+    if ((rc = common_args(lors, n, lor_stride, images, image_strides, images_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
+    if ((rc = batch_args(n_images, batch_stride, values_stride, n, v, vt, g))) return rc;
+    if (n > 0 && !values) return fail(SRF_EINVAL, "values must not be NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (tof) {
+        TofParams tp;
+        if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
+        return launch_batch_trace<true, SCATTER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, n_images, batch_stride, values, nullptr, values_stride, s);
+    }
+    TofParams tp{0, 0, 0};
+    return launch_batch_trace<false, SCATTER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, n_images, batch_stride, values, nullptr, values_stride, s);
 }
 
 int srf_count_pairs(const float *lors, int64_t n, int32_t lor_stride, const float *tof,

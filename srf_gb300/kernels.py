@@ -121,6 +121,53 @@ def backproject(lors: torch.Tensor, values: torch.Tensor, shape, center, size, *
     return acc
 
 
+MAX_BATCH = 8
+
+
+def project_batch(lors: torch.Tensor, images: torch.Tensor, center, size, *,
+                  tof: Optional[Tuple[float, float]] = None, tof_nsigma: float = 0.0) -> torch.Tensor:
+    """(B, N) projections of a batch of (nx, ny, nz) images (B <= 8), one traversal per LOR."""
+    n, stride = check_lors(lors, tof is not None)
+    _require_cuda(images, "images")
+    if images.dim() != 4 or not 1 <= images.shape[0] <= MAX_BATCH:
+        raise ValueError(f"images must be (B <= {MAX_BATCH}, nx, ny, nz)")
+    B, nx, ny, nz = images.shape
+    xb = images.permute(0, 3, 2, 1).contiguous()             # (B, nz, ny, nx): x fastest
+    yb = images.permute(0, 3, 1, 2).contiguous()             # (B, nz, nx, ny): y fastest
+    out = torch.empty((B, n), dtype=F32, device=lors.device)
+    tof_p = _tof_ptr(lors) if tof is not None else None
+    tb, tsg = tof if tof is not None else (0.0, 0.0)
+    call("srf_projection_batch", ptr(lors), i64(n), i32(stride), tof_p, i32(stride),
+         *_tof_args(tb, tsg, tof_nsigma), i32(B), i64(nx * ny * nz), ptr(xb), i64x3((1, nx, nx * ny)),
+         ptr(yb), i64x3((ny, 1, nx * ny)), i32x3((nx, ny, nz)), f32x3(center), f32x3(size), ptr(out),
+         i64(n), stream_ptr(lors.device))
+    return out
+
+
+def adjoint_batch(lors: torch.Tensor, values: torch.Tensor, shape, center, size, *,
+                  tof: Optional[Tuple[float, float]] = None, tof_nsigma: float = 0.0) -> torch.Tensor:
+    """(B, nx, ny, nz) exact adjoint of ``project_batch`` for (B, N) LOR values."""
+    n, stride = check_lors(lors, tof is not None)
+    _require_cuda(values, "values")
+    values = values.contiguous()
+    if values.dim() != 2 or values.shape[1] != n or not 1 <= values.shape[0] <= MAX_BATCH:
+        raise ValueError(f"values must be (B <= {MAX_BATCH}, N)")
+    B = values.shape[0]
+    nx, ny, nz = shape
+    acc = torch.zeros((B, nz, ny, nx), dtype=F32, device=lors.device)
+    acc_t = torch.zeros((B, nz, nx, ny), dtype=F32, device=lors.device)
+    tof_p = _tof_ptr(lors) if tof is not None else None
+    tb, tsg = tof if tof is not None else (0.0, 0.0)
+    call("srf_projection_adjoint_batch", ptr(lors), i64(n), i32(stride), tof_p, i32(stride),
+         *_tof_args(tb, tsg, tof_nsigma), i32(B), ptr(values), i64(n), ptr(acc), i64(nx * ny * nz),
+         i64x3((1, nx, nx * ny)), ptr(acc_t), i64x3((ny, 1, nx * ny)), i32x3(shape), f32x3(center),
+         f32x3(size), stream_ptr(lors.device))
+    out = acc.permute(0, 3, 2, 1)                             # (B, nx, ny, nz) views, x fastest
+    for b in range(B):
+        fold(out[b], acc_t[b].permute(1, 2, 0))
+    return out
+
+
 def count_pairs(lors: torch.Tensor, shape, center, size, *, rules: int,
                 tof: Optional[Tuple[float, float]] = None, tof_nsigma: float = 0.0) -> int:
     """Exact number of (LOR, voxel) visits of the projector (rules=0) or backprojector (1)."""

@@ -71,7 +71,6 @@ class CoarseGeometry:
         self.bin_lors = torch.as_tensor(lors.astype(np.float32), device=self.device)
         self.ic = ImageConfig(list(VOL_SHAPE), [0.0, 0.0, 0.0], list(FOV_MM))
         self.scatter_points = self._scatter_points()
-        self.coarse_points = self._coarse_points()
 
     def _scatter_points(self) -> np.ndarray:
         """Every floor(50 mm / voxel) voxels, as preprocess.py:6-18 places them."""
@@ -79,16 +78,6 @@ class CoarseGeometry:
         from .data import Image
         img = Image(np.zeros(VOL_SHAPE, np.float32), self.ic.center, self.ic.size)
         return pre_all_scatter_position(img)
-
-    def _coarse_points(self) -> np.ndarray:
-        """The centres of 2 x 2 transaxial groups of the SSS scatter points (all axial layers): a
-        quarter of the points, spread over the same region (input of the learned surrogate)."""
-        p = self.scatter_points
-        xs, ys, zs = (np.unique(p[:, c]) for c in range(3))
-        cx = 0.5 * (xs[0::2][: len(xs) // 2] + xs[1::2][: len(xs) // 2])
-        cy = 0.5 * (ys[0::2][: len(ys) // 2] + ys[1::2][: len(ys) // 2])
-        X, Y, Z = np.meshgrid(cx, cy, zs, indexing="ij")
-        return np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1).astype(np.float32)
 
     def n_bins(self) -> int:
         return self.pairs.shape[0]
@@ -160,15 +149,13 @@ def random_phantom(seed: int, device="cuda") -> Tuple[torch.Tensor, torch.Tensor
 
 def sss_sinogram(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor,
                  low: int = 350, high: int = 650, resolution: float = 0.15,
-                 bins: torch.Tensor = None, points: torch.Tensor = None) -> torch.Tensor:
+                 bins: torch.Tensor = None) -> torch.Tensor:
     """Raw SSS sums of every bin (or of the bins listed) as a flat FP32 tensor.
 
     The preprocessing of preprocess.py (emission line integrals x L^2 and attenuation factors
     from every detector to every scatter point, detector-major) runs on the GPU projector; with
-    ``bins`` only the virtual crystals those bins touch are preprocessed. ``points`` replaces the
-    scatter points (default: the reference's every-50-mm grid)."""
-    sp = torch.as_tensor(geo.scatter_points if points is None else points, dtype=torch.float32,
-                         device=geo.device)
+    ``bins`` only the virtual crystals those bins touch are preprocessed."""
+    sp = torch.as_tensor(geo.scatter_points, dtype=torch.float32, device=geo.device)
     ic = geo.ic
     pairs = geo.pairs_dev if bins is None else geo.pairs_dev.index_select(0, bins)
     if bins is None:
@@ -199,7 +186,7 @@ def sss_sinogram(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor,
 PAD_GRID = (56, 56, 320)
 VIEW_PAD = 4
 HALF_GRID = (28, 28, 160)
-N_FEATURES = 15
+N_FEATURES = 16   # 9 measured + 7 geometry channels
 
 
 def pad_sino(g: torch.Tensor) -> torch.Tensor:
@@ -225,76 +212,67 @@ def full_mask(device) -> torch.Tensor:
 
 def _half_cells(geo: CoarseGeometry):
     """Per half-resolution cell (28 x 28 x 160, flattened): the bin it samples (plane 2z, radial
-    2y, view 2x - 4, clamped/wrapped like the padding), that bin's LOR, and the constant input
-    channels (radial and plane coordinates in [-1, 1], 1 on cells over real bins)."""
+    2y, view 2x - 4, clamped/wrapped like the padding), that bin's LOR, the constant input
+    channels (LOR midpoint, direction harmonics, plane coordinate) and the cell's virtual
+    crystals."""
     if getattr(geo, "_half", None) is None:
         dev = geo.device
         pz = torch.clamp(torch.arange(HALF_GRID[0], device=dev) * 2, max=PLANES - 2)
         ry = torch.clamp(torch.arange(HALF_GRID[1], device=dev) * 2, max=RADIAL - 1)
         vx = (torch.arange(HALF_GRID[2], device=dev) * 2 - VIEW_PAD) % VIEWS
         idx = ((pz[:, None, None] * RADIAL + ry[None, :, None]) * VIEWS + vx[None, None, :]).reshape(-1)
-        shape = HALF_GRID
-        rc = ((ry.float() - (RADIAL - 1) / 2) / ((RADIAL - 1) / 2))[None, :, None].expand(shape)
-        pc = ((pz.float() - (PLANES - 2) / 2) / ((PLANES - 2) / 2))[:, None, None].expand(shape)
-        real = torch.zeros(shape, device=dev)
-        real[: PLANES // 2, : RADIAL // 2, VIEW_PAD // 2: (VIEW_PAD + VIEWS) // 2] = 1.0
-        const = torch.stack([rc, pc, real], -1).reshape(-1, 3)
-        geo._half = (idx, geo.bin_lors.index_select(0, idx).contiguous(), const)
+        L = geo.bin_lors.index_select(0, idx).contiguous()
+        pc = ((pz.float() - (PLANES - 2) / 2) / ((PLANES - 2) / 2))[:, None, None].expand(HALF_GRID).reshape(-1)
+        xm, ym = (L[:, 0] + L[:, 3]) / 600.0, (L[:, 1] + L[:, 4]) / 600.0
+        th = torch.atan2(L[:, 4] - L[:, 1], L[:, 3] - L[:, 0])
+        const = torch.stack([xm, ym, torch.cos(2 * th), torch.sin(2 * th), torch.cos(4 * th),
+                             torch.sin(4 * th), pc], -1)
+        pr = geo.pairs_dev.index_select(0, idx).long()
+        geo._half = (idx, L, const, pr[:, 0].contiguous(), pr[:, 1].contiguous())
     return geo._half
 
 
-def coarse_sss_points(geo: CoarseGeometry, mu: torch.Tensor) -> torch.Tensor:
-    """The coarse scatter points whose nearest voxel has mu > 0 (the others add exactly 0)."""
-    pts = torch.as_tensor(geo.coarse_points, device=mu.device)
-    shape = torch.tensor(mu.shape, device=mu.device)
-    size = torch.tensor(geo.ic.size, dtype=torch.float32, device=mu.device)
-    idx = ((pts / size + 0.5) * shape).long()
-    idx = torch.minimum(torch.clamp(idx, min=0), shape - 1)
-    keep = mu[idx[:, 0], idx[:, 1], idx[:, 2]] > 0
-    return pts[keep].contiguous()
-
-
-def network_input(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor,
-                  coarse_scale: float = 1.0) -> Tuple[torch.Tensor, float]:
+def network_input(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor) -> Tuple[torch.Tensor, float]:
     """(1, 28, 28, 160, 16) bfloat16 network input and the emission scale.
 
-    Each half-resolution cell samples one bin's LOR. Local channels: emission line integral / its
-    mean over the cells (e), attenuation factor (a), e * a, the mu line integral / 4 (m), and a
-    cheap SSS of the cell's bin over a quarter of the scatter points (coarse_sss_points), in units
-    of the emission scale / coarse_scale. Context channels (scatter at a bin sums over the whole
-    object, more than a 3-level U-Net sees): e, a and e * a averaged over the views of the cell's
-    (plane, radial) row, e and m averaged over its plane, e * a and m averaged over all cells.
-    Geometry channels: the radial and plane coordinates, 1 on cells over real bins. Targets and
+    Each half-resolution cell samples one bin's LOR (virtual crystals A, B). Local channels:
+    emission line integral / its mean over the cells (e), attenuation factor (a), e * a, the mu
+    line integral / 4 (m). Detector channels: single scatter into a bin sums, over scatter points,
+    emission along lines from A and from B, so for each virtual crystal the sums of e and e * a
+    over every cell it belongs to (what that detector sees of the object) are given at A and at B,
+    each / its mean over crystals. Context: e averaged over the views of the cell's (plane,
+    radial) row. Geometry: the scatter points sit on a Cartesian grid, so the target is not
+    rotation-equivariant in the views; the LOR's midpoint (x, y) / 300 mm, the 2nd and 4th
+    harmonics of its direction and the plane coordinate locate each cell absolutely. Targets and
     predictions are in units of the emission scale, so the network is scale-free."""
-    idx, L, const = _half_cells(geo)
+    idx, L, const, ca, cb = _half_cells(geo)
     ic = geo.ic
     p = kernels.project(L, kernels.xfast(emission), ic.center, ic.size)
     len2 = ((L[:, 3] - L[:, 0]) ** 2 + (L[:, 4] - L[:, 1]) ** 2 + (L[:, 5] - L[:, 2]) ** 2)
     e = p * len2
     a = kernels.attenuation(L, kernels.xfast(mu), ic.center, ic.size)
     scale = float(e.mean().item())
-    pts = coarse_sss_points(geo, mu)
-    if pts.shape[0] > 0:
-        cs = sss_sinogram(geo, emission, mu, bins=idx, points=pts)
-    else:
-        cs = torch.zeros_like(e)
-    cs = (cs / (max(scale, 1e-30) * coarse_scale)).reshape(HALF_GRID)
-    en = (e / max(scale, 1e-30)).reshape(HALF_GRID)
-    a = a.reshape(HALF_GRID)
+    en = e / max(scale, 1e-30)
     ea = en * a
     m = -torch.log(torch.clamp(a, min=1e-30)) * 0.25
-    row = lambda t: t.mean(dim=2, keepdim=True).expand(HALF_GRID)
-    plane = lambda t: t.mean(dim=(1, 2), keepdim=True).expand(HALF_GRID)
-    glob = lambda t: t.mean().expand(HALF_GRID)
-    feats = [en, a, ea, m, cs, row(en), row(a), row(ea), plane(en), plane(m), glob(ea), glob(m)]
-    x = torch.empty((*HALF_GRID, 16), dtype=torch.bfloat16, device=L.device)
-    x[..., :len(feats)] = torch.stack(feats, -1).to(torch.bfloat16)
-    x[..., len(feats):len(feats) + 3] = const.reshape(*HALF_GRID, 3).to(torch.bfloat16)
-    x[..., len(feats) + 3:] = 0
-    return x.reshape(1, *HALF_GRID, 16), scale
+    n_c = geo.vpos.shape[0]
 
+    def per_detector(v):
+        t = torch.zeros(n_c, dtype=torch.float32, device=v.device)
+        t.index_add_(0, ca, v)
+        t.index_add_(0, cb, v)
+        t = t / t.mean().clamp_min(1e-30)
+        return t.index_select(0, ca), t.index_select(0, cb)
 
-COARSE_CHANNEL = 4
+    fa, fb = per_detector(en)
+    ga, gb = per_detector(ea)
+    H = HALF_GRID
+    row = lambda t: t.reshape(H).mean(dim=2, keepdim=True).expand(H).reshape(-1)
+    feats = [en, a, ea, m, fa, fb, ga, gb, row(en)]
+    x = torch.empty((L.shape[0], 16), dtype=torch.bfloat16, device=L.device)
+    x[:, :len(feats)] = torch.stack(feats, 1).to(torch.bfloat16)
+    x[:, len(feats):] = const.to(torch.bfloat16)
+    return x.reshape(1, *H, 16), scale
 
 
 def target_full(sino_flat: torch.Tensor, scale: float) -> torch.Tensor:

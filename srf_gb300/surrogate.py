@@ -274,20 +274,20 @@ class ScatterSurrogate:
     on ``spot_bins`` random bins, and whether that exceeded ``fallback_tol`` so that the full SSS
     was returned instead."""
 
-    def __init__(self, geo, net: UNet3D, target_scale: float, coarse_scale: float = 1.0,
-                 fallback_tol: float = 0.05, spot_bins: int = 2048, seed: int = 0):
-        self.geo, self.net, self.k, self.kc = geo, net, float(target_scale), float(coarse_scale)
+    def __init__(self, geo, net: UNet3D, target_scale: float, fallback_tol: float = 0.05,
+                 spot_bins: int = 2048, seed: int = 0):
+        self.geo, self.net, self.k = geo, net, float(target_scale)
         self.fallback_tol, self.spot_bins = fallback_tol, spot_bins
         self.gen = torch.Generator(device=geo.device).manual_seed(seed)
 
     @classmethod
     def load(cls, geo, path: str = DEFAULT_WEIGHTS, **kw) -> "ScatterSurrogate":
         net, meta = load_weights(path, geo.device)
-        return cls(geo, net, meta["target_scale"], meta.get("coarse_scale", 1.0), **kw)
+        return cls(geo, net, meta["target_scale"], **kw)
 
     def predict(self, emission: torch.Tensor, mu: torch.Tensor) -> torch.Tensor:
         from .scatter_sinogram import crop_sino, network_input
-        inp, scale = network_input(self.geo, emission, mu, self.kc)
+        inp, scale = network_input(self.geo, emission, mu)
         out = self.net.forward(inp)                                     # (1, 56, 56, 320)
         return crop_sino(out)[0] * (self.k * scale)
 
@@ -321,7 +321,7 @@ class ScatterSurrogate:
 
 
 # ---------------------------------------------------------------- training
-def build_dataset(geo, seeds, log=None, coarse_scale: float = 1.0):
+def build_dataset(geo, seeds, log=None):
     """Network inputs (N, 28, 28, 160, 16) bf16, targets (N, 56, 56, 320) FP32 in units of each
     study's emission scale, and the scales."""
     from .scatter_sinogram import HALF_GRID, PAD_GRID, network_input, random_phantom, sss_sinogram, target_full
@@ -333,7 +333,7 @@ def build_dataset(geo, seeds, log=None, coarse_scale: float = 1.0):
     for i, sd in enumerate(seeds):
         em, mu = random_phantom(int(sd), device=dev)
         sc = sss_sinogram(geo, em, mu)
-        inp, scale = network_input(geo, em, mu, coarse_scale)
+        inp, scale = network_input(geo, em, mu)
         X[i] = inp[0]
         T[i] = target_full(sc, scale)
         scales[i] = scale
@@ -392,7 +392,7 @@ def main(argv=None) -> None:
     import json
     import time
     from . import synth
-    from .scatter_sinogram import COARSE_CHANNEL, CoarseGeometry, full_mask
+    from .scatter_sinogram import CoarseGeometry, full_mask
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--train", type=int, default=2000)
@@ -412,12 +412,9 @@ def main(argv=None) -> None:
     mask = full_mask(dev)
     k = float(((T * mask).sum() / (mask.sum() * T.shape[0])).item())
     T /= k
-    # the coarse-SSS input channel in units of its own dataset mean
-    kc = float(X[..., COARSE_CHANNEL].float().mean().item())
-    X[..., COARSE_CHANNEL] = (X[..., COARSE_CHANNEL].float() / kc).to(BF16)
     net = UNet3D(channels=tuple(int(c) for c in a.channels.split(",")), seed=1, device=dev)
     log(f"parameters {net.n_params()}")
-    sur = ScatterSurrogate(geo, net, k, kc)
+    sur = ScatterSurrogate(geo, net, k)
     mon = range(1_000_000, 1_000_000 + 10)
 
     def every(ep):
@@ -431,7 +428,7 @@ def main(argv=None) -> None:
     t_train = time.time() - t0
     del X, T
     errs = evaluate(sur, range(1_000_000, 1_000_000 + a.held_out))
-    meta = {"target_scale": k, "coarse_scale": kc, "train_studies": a.train, "epochs": a.epochs, "train_s": t_train,
+    meta = {"target_scale": k, "train_studies": a.train, "epochs": a.epochs, "train_s": t_train,
             "held_out_mean_rel_l2": sum(errs) / len(errs), "held_out_max_rel_l2": max(errs)}
     save_weights(net, a.out, meta)
     print(json.dumps({**meta, "loss_history": hist}))

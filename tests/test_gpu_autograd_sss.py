@@ -60,6 +60,35 @@ def test_batched_projector_adjoint_identity(cuda_lib, small_case):
     assert abs(lhs - rhs) / abs(lhs) <= 1e-6
 
 
+@pytest.mark.parametrize("tof", [False, True])
+def test_batched_projector_matches_single_image_kernels(cuda_lib, small_case, tof):
+    """srf_projection_batch / srf_projection_adjoint_batch against the single-image kernels, for
+    a batch of 8 and a batch of 11 (split 8 + 3) through the autograd path."""
+    from srf_gb300 import autograd, kernels
+    ic, sc = small_case["ic"], small_case["scanner"]
+    dev = torch.device("cuda", 0)
+    lors = torch.as_tensor(small_case["lors"], device=dev)
+    t = (sc.tof.tof_bin, sc.tof.tof_sigma2) if tof else None
+    rng = np.random.default_rng(3)
+    xb = torch.as_tensor(rng.random((8, *ic.shape)).astype(np.float32), device=dev)
+    pb = kernels.project_batch(lors, xb, ic.center, ic.size, tof=t)
+    for b in range(8):
+        ps = kernels.project(lors, xb[b], ic.center, ic.size, tof=t)
+        assert rel_l2(pb[b].cpu().numpy(), ps.cpu().numpy()) <= 1e-6
+    vb = torch.as_tensor(rng.random((8, lors.shape[0])).astype(np.float32), device=dev)
+    gb = kernels.adjoint_batch(lors, vb, ic.shape, ic.center, ic.size, tof=t)
+    for b in range(8):
+        gs = kernels.backproject(lors, vb[b], ic.shape, ic.center, ic.size, tof=t, adjoint=True)
+        assert rel_l2(gb[b].cpu().numpy(), gs.cpu().numpy()) <= 1e-5
+    x11 = torch.as_tensor(rng.random((11, *ic.shape)).astype(np.float32), device=dev).requires_grad_(True)
+    p11 = autograd.project(x11, lors, ic.center, ic.size, tof=t)
+    y11 = torch.as_tensor(rng.random(p11.shape).astype(np.float32), device=dev)
+    (p11 * y11).sum().backward()
+    lhs = float((p11.detach().double() * y11.double()).sum())
+    rhs = float((x11.detach().double() * x11.grad.double()).sum())
+    assert abs(lhs - rhs) / abs(lhs) <= 1e-6
+
+
 def test_sss_kernel_matches_oracle(cuda_lib, oracle):
     import os
     from srf_gb300 import kernels

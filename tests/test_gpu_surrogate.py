@@ -49,7 +49,7 @@ def test_wrong_network_falls_back_to_sss(geo):
     from srf_gb300.surrogate import DEFAULT_WEIGHTS, ScatterSurrogate, load_weights
     net, meta = load_weights(DEFAULT_WEIGHTS, geo.device)
     net.hb += 3.0  # shifts every prediction far from the SSS sinogram
-    bad = ScatterSurrogate(geo, net, meta["target_scale"], meta["coarse_scale"])
+    bad = ScatterSurrogate(geo, net, meta["target_scale"])
     em, mu = random_phantom(1_000_103, device=geo.device)
     est, info = bad.estimate(em, mu)
     assert info["fallback"] and info["spot_rel_l2"] > 0.05
