@@ -305,11 +305,13 @@ static int batch_args(int32_t n_images, int64_t batch_stride, int64_t row_stride
                       const View &v, const View &vt, const Grid &g) {
     if (n_images < 1 || n_images > kMaxBatch) return fail(SRF_EINVAL, "n_images must be 1..%d", kMaxBatch);
     if (row_stride < n) return fail(SRF_EINVAL, "row stride of the LOR values is below n");
-    int64_t span = 0;  // largest element offset within one image (either layout)
+    int64_t span_v = 0, span_t = 0;  // largest element offset within one image, per layout
     for (int k = 0; k < 3; ++k) {
-        const int nk = k == 0 ? g.nx : (k == 1 ? g.ny : g.nz);
-        span += (nk - 1) * (v.st[k] > vt.st[k] ? v.st[k] : vt.st[k]);
+        const int64_t nk = k == 0 ? g.nx : (k == 1 ? g.ny : g.nz);
+        span_v += (nk - 1) * v.st[k];
+        span_t += (nk - 1) * vt.st[k];
     }
+    const int64_t span = span_v > span_t ? span_v : span_t;
     if (n_images > 1 && batch_stride <= span) return fail(SRF_EGRID, "images of the batch overlap");
     return SRF_OK;
 }
