@@ -278,7 +278,7 @@ int srf_emap_block_full(const float *crystal_table, int32_t n_blocks, int32_t m,
  * kn_formula.py:6-20, including the reference's whole-degree angle quantisation and its use of
  * the angle inside fkn):
  *   pairs          int32 (a, b) crystal ids, n_pairs rows
- *   crystal_pos    float32 (n_crystals, 3); scatter_pos float32 (n_scatter, 3)
+ *   crystal_pos    float32 (n_crystals, 3); scatter_pos float32 (n_scatter, 3), n_scatter <= 12288
  *   sumup_emission, atten  float32 (n_crystals, n_scatter), crystal-major
  *   umap           float32 (shape0, shape1, shape2) C order, umap_size mm
  * Outputs scatter[k] and scale[k] before the host scaling of scatter_fraction.py:27-36. */

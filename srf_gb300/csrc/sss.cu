@@ -16,15 +16,18 @@
 // GB300 design: because theta is quantised to whole degrees, cos theta, 511/E', eff(E') and the
 // Klein-Nishina factor take at most 181 values; each block builds those tables in shared memory
 // (double precision, then rounded) and the inner loop is table lookups plus two power
-// functions. One warp per LOR pair, lanes over scatter points, so the crystal-major emission and
-// attenuation rows are read coalesced. The angle is evaluated in FP32 and re-evaluated in FP64
-// when it falls within 0.01 degree of a whole degree or |cos| > 0.999, so its quantisation
-// agrees with a double-precision evaluation.
+// functions; mu at each scatter point's nearest voxel is looked up once per block into shared
+// memory. One warp per LOR pair, lanes over scatter points, so the crystal-major emission and
+// attenuation rows are read coalesced. The angle is evaluated in FP32 with a bound on its
+// rounding error (from the law-of-cosines operands and acosf's accuracy) and re-evaluated in
+// FP64 only when a whole degree lies within four times that bound, so its quantisation agrees
+// with a double-precision evaluation while the slow path stays rare.
 #include "common.cuh"
 
 namespace srf {
 
 constexpr int kAngles = 181;
+constexpr int kMaxScatterPoints = 12288;  // their mu values fill at most 48 KB of shared memory
 
 __device__ __forceinline__ double block_theta_d(int ncpr, int nbpr, int gb1, double px, double py, double pz) {
     const double norm = sqrt(px * px + py * py + pz * pz);
@@ -43,6 +46,18 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
       float us0, float us1, float us2, int ncpr, int nbpr, int gb1, int low, int high, double res,
       float *__restrict__ scatter, float *__restrict__ scale) {
     __shared__ float t_g[kAngles], t_eff[kAngles], t_fk[kAngles];
+    extern __shared__ float s_mu[];  // n_s entries: mu at the nearest voxel of each scatter point
+    for (int t = threadIdx.x; t < n_s; t += blockDim.x) {
+        // kn_formula.py:12-14; outside the map counts as 0
+        const float sx = __ldg(spos + 3 * t), sy = __ldg(spos + 3 * t + 1), sz = __ldg(spos + 3 * t + 2);
+        const int g0 = (int)((sx / us0 + 0.5f) * u0);
+        const int g1 = (int)((sy / us1 + 0.5f) * u1);
+        const int g2 = (int)((sz / us2 + 0.5f) * u2);
+        float mu = 0.0f;
+        if (g0 >= 0 && g0 < u0 && g1 >= 0 && g1 < u1 && g2 >= 0 && g2 < u2)
+            mu = __ldg(umap + ((int64_t)g0 * u1 + g1) * u2 + g2);
+        s_mu[t] = mu;
+    }
     for (int t = threadIdx.x; t < kAngles; t += blockDim.x) {
         const double ang = (double)t / 180.0 * M_PI;
         const double c = cos(ang);
@@ -85,12 +100,23 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
             const float as2 = dax * dax + day * day + daz * daz;
             const float sb2 = dbx * dbx + dby * dby + dbz * dbz;
             const float as = sqrtf(as2), sb = sqrtf(sb2);
-            float arg = -(as2 + sb2 - ab2) / (2.0f * as * sb);
+            const float den = 2.0f * as * sb;
+            float arg = -(as2 + sb2 - ab2) / den;
             arg = fminf(1.0f, fmaxf(-1.0f, arg));
-            float deg = acosf(arg) * (float)(180.0 / M_PI);
-            const float fr = deg - floorf(deg);
+            // |error of arg| <= 7u (as2 + sb2 + ab2) / den + 9u (u = 2^-24); acosf is within 5e-7
+            // rad and the degree conversion within 2.2e-5 degree
+            const float E = 5.0e-7f * (as2 + sb2 + ab2) / den + 6.0e-7f;
+            const float m = fabsf(arg) + E;
+            bool slow = m >= 0.9999f;
+            float deg = 0.0f;
+            if (!slow) {
+                deg = acosf(arg) * (float)(180.0 / M_PI);
+                const float tol = 4.0f * (57.2957795f * (E * rsqrtf(1.0f - m * m) + 5.0e-7f) + 2.2e-5f);
+                const float fr = deg - floorf(deg);
+                slow = fr < tol || fr > 1.0f - tol;
+            }
             int ti;
-            if (fr < 0.01f || fr > 0.99f || fabsf(arg) > 0.999f) {
+            if (slow) {
                 const double Dax = (double)ax - sx, Day = (double)ay - sy, Daz = (double)az - sz;
                 const double Dbx = (double)bx - sx, Dby = (double)by - sy, Dbz = (double)bz - sz;
                 const double Dab = sqrt((double)dabx * dabx + (double)daby * daby + (double)dabz * dabz);
@@ -103,13 +129,7 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
                 ti = (int)deg;
             }
             ti = min(max(ti, 0), kAngles - 1);
-            // mu at the nearest voxel of S (kn_formula.py:12-14); outside the map counts as 0
-            const int g0 = (int)((sx / us0 + 0.5f) * u0);
-            const int g1 = (int)((sy / us1 + 0.5f) * u1);
-            const int g2 = (int)((sz / us2 + 0.5f) * u2);
-            float mu = 0.0f;
-            if (g0 >= 0 && g0 < u0 && g1 >= 0 && g1 < u1 && g2 >= 0 && g2 < u2)
-                mu = __ldg(umap + ((int64_t)g0 * u1 + g1) * u2 + g2);
+            const float mu = s_mu[s];
             const float gexp = t_g[ti];
             const float a_a = __ldg(ata + s), a_b = __ldg(atb + s);
             const float Ia = a_a * exp2f(__log2f(a_b) * gexp) * __ldg(ema + s);
@@ -155,9 +175,11 @@ extern "C" int srf_sss(const int32_t *pairs, int64_t n_pairs, const float *cryst
     }
     if (!std::isfinite(resolution) || !(resolution > 0)) return fail(SRF_ENONFINITE, "resolution must be > 0");
     if (high_energy - low_energy > 5 * 100000) return fail(SRF_ERANGE, "energy window too wide");
+    if (n_scatter > kMaxScatterPoints) return fail(SRF_ERANGE, "at most %d scatter points", kMaxScatterPoints);
     const double res = sqrt(511.0) * (double)resolution;
-    unsigned blocks = grid_for(k_sss, n_pairs, kBlock / 32);
-    k_sss<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(
+    const int smem = n_scatter * (int)sizeof(float);
+    unsigned blocks = grid_for(k_sss, n_pairs, kBlock / 32, smem);
+    k_sss<<<blocks, kBlock, smem, (cudaStream_t)stream>>>(
         pairs, n_pairs, n_crystals, crystal_pos, scatter_pos, n_scatter, sumup_emission, atten, umap,
         umap_shape[0], umap_shape[1], umap_shape[2], umap_size[0], umap_size[1], umap_size[2],
         nb_crystals_per_ring, nb_blocks_per_ring, grid_block[1], low_energy, high_energy, res,
