@@ -155,15 +155,20 @@ def sss_sinogram(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor,
     The preprocessing of preprocess.py (emission line integrals x L^2 and attenuation factors
     from every detector to every scatter point, detector-major) runs on the GPU projector; with
     ``bins`` only the virtual crystals those bins touch are preprocessed."""
+    if bins is None:
+        return sss_pairs(geo, emission, mu, geo.vpos_dev, geo.pairs_dev, low, high, resolution)
+    pairs = geo.pairs_dev.index_select(0, bins)
+    uniq, inv = torch.unique(pairs.reshape(-1), return_inverse=True)
+    return sss_pairs(geo, emission, mu, geo.vpos_dev.index_select(0, uniq),
+                     inv.reshape(-1, 2).to(torch.int32), low, high, resolution)
+
+
+def sss_pairs(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor, cpos: torch.Tensor,
+              pairs: torch.Tensor, low: int = 350, high: int = 650, resolution: float = 0.15) -> torch.Tensor:
+    """SSS of crystal pairs given as int32 indices into the crystal positions ``cpos`` (m, 3):
+    preprocessing of those m crystals, then srf_sss. No host synchronisation."""
     sp = torch.as_tensor(geo.scatter_points, dtype=torch.float32, device=geo.device)
     ic = geo.ic
-    pairs = geo.pairs_dev if bins is None else geo.pairs_dev.index_select(0, bins)
-    if bins is None:
-        cpos = geo.vpos_dev
-    else:
-        uniq, inv = torch.unique(pairs.reshape(-1), return_inverse=True)
-        cpos = geo.vpos_dev.index_select(0, uniq)
-        pairs = inv.reshape(-1, 2).to(torch.int32)
     m, k = cpos.shape[0], sp.shape[0]
     Ld = torch.cat([cpos[:, None, :].expand(m, k, 3), sp[None, :, :].expand(m, k, 3)], 2).reshape(-1, 6)
     Ld = Ld.contiguous()
@@ -232,8 +237,9 @@ def _half_cells(geo: CoarseGeometry):
     return geo._half
 
 
-def network_input(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor) -> Tuple[torch.Tensor, float]:
-    """(1, 28, 28, 160, 16) bfloat16 network input and the emission scale.
+def network_input(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor) -> Tuple[torch.Tensor, torch.Tensor]:
+    """(1, 28, 28, 160, 16) bfloat16 network input and the emission scale (a device scalar, so
+    that nothing waits for the GPU).
 
     Each half-resolution cell samples one bin's LOR (virtual crystals A, B). Local channels:
     emission line integral / its mean over the cells (e), attenuation factor (a), e * a, the mu
@@ -251,8 +257,8 @@ def network_input(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor)
     len2 = ((L[:, 3] - L[:, 0]) ** 2 + (L[:, 4] - L[:, 1]) ** 2 + (L[:, 5] - L[:, 2]) ** 2)
     e = p * len2
     a = kernels.attenuation(L, kernels.xfast(mu), ic.center, ic.size)
-    scale = float(e.mean().item())
-    en = e / max(scale, 1e-30)
+    scale = e.mean().clamp_min(1e-30)
+    en = e / scale
     ea = en * a
     m = -torch.log(torch.clamp(a, min=1e-30)) * 0.25
     n_c = geo.vpos.shape[0]

@@ -27,6 +27,7 @@ import ctypes
 import math
 from typing import Dict, List, Optional, Tuple
 
+import numpy as np
 import torch
 
 from ._lib import call, f32, i32, i64, ptr, stream_ptr
@@ -272,49 +273,103 @@ class ScatterSurrogate:
     ``estimate(emission, mu)`` returns the flat (51 * 52 * 312) scatter sinogram in SSS units and
     a record of what happened: the relative L2 difference between the prediction and a fresh SSS
     on ``spot_bins`` random bins, and whether that exceeded ``fallback_tol`` so that the full SSS
-    was returned instead."""
+    was returned instead. The spot-check SSS runs on a side stream while the network runs on the
+    caller's stream; the only host synchronisation is the final comparison."""
+
+    N_POOLS = 8
+    POOL_POSITIONS = 48
 
     def __init__(self, geo, net: UNet3D, target_scale: float, fallback_tol: float = 0.05,
                  spot_bins: int = 2048, seed: int = 0):
         self.geo, self.net, self.k = geo, net, float(target_scale)
         self.fallback_tol, self.spot_bins = fallback_tol, spot_bins
         self.gen = torch.Generator(device=geo.device).manual_seed(seed)
+        self.side = torch.cuda.Stream(geo.device)
+        self.pools = self._make_pools(seed)
+        self.calls = 0
+        self._graph = self._graph_in = self._graph_out = None
+
+    def _make_pools(self, seed: int):
+        """Spot-check pools, built once: each is a random set of 48 of the 312 transaxial
+        positions (all rings), its 1,248 virtual crystals and every bin whose two crystals lie in
+        it (as indices into those crystals). A spot check samples bins of one pool, so its SSS
+        preprocesses 1,248 crystals instead of 8,112 while the bins still cover every plane,
+        radius and 48 views."""
+        geo = self.geo
+        rng = np.random.default_rng(seed)
+        pools = []
+        pairs = geo.pairs.astype(np.int64)
+        for _ in range(self.N_POOLS):
+            pos = np.sort(rng.choice(geo.vt, self.POOL_POSITIONS, replace=False))
+            crystals = (np.arange(geo.vr)[:, None] * geo.vt + pos[None, :]).reshape(-1)
+            local = np.full(geo.vt * geo.vr, -1, np.int64)
+            local[crystals] = np.arange(crystals.size)
+            la, lb = local[pairs[:, 0]], local[pairs[:, 1]]
+            cand = np.flatnonzero((la >= 0) & (lb >= 0))
+            dev = geo.device
+            pools.append((torch.as_tensor(cand, device=dev),
+                          torch.as_tensor(np.stack([la[cand], lb[cand]], 1).astype(np.int32), device=dev),
+                          geo.vpos_dev.index_select(0, torch.as_tensor(crystals, device=dev))))
+        return pools
 
     @classmethod
     def load(cls, geo, path: str = DEFAULT_WEIGHTS, **kw) -> "ScatterSurrogate":
         net, meta = load_weights(path, geo.device)
         return cls(geo, net, meta["target_scale"], **kw)
 
+    def _forward(self, inp: torch.Tensor) -> torch.Tensor:
+        """The network's forward pass, replayed from a CUDA graph captured at the first call
+        (the ~30 launches of one inference cost more to issue than to run at batch 1)."""
+        if self._graph is None or self._graph_in.shape != inp.shape:
+            self._graph_in = inp.clone()
+            side = torch.cuda.Stream(inp.device)
+            side.wait_stream(torch.cuda.current_stream(inp.device))
+            with torch.cuda.stream(side):
+                self.net.forward(self._graph_in)  # allocates the activation buffers
+            torch.cuda.current_stream(inp.device).wait_stream(side)
+            self._graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self._graph):
+                self._graph_out = self.net.forward(self._graph_in)
+            # the graph writes into these activation buffers: keep them alive even if the network
+            # later reallocates its buffers for another batch shape
+            self._graph_bufs = dict(self.net.buf)
+        self._graph_in.copy_(inp)
+        self._graph.replay()
+        return self._graph_out
+
     def predict(self, emission: torch.Tensor, mu: torch.Tensor) -> torch.Tensor:
         from .scatter_sinogram import crop_sino, network_input
         inp, scale = network_input(self.geo, emission, mu)
-        out = self.net.forward(inp)                                     # (1, 56, 56, 320)
+        out = self._forward(inp)                                        # (1, 56, 56, 320)
         return crop_sino(out)[0] * (self.k * scale)
 
-    def draw_spot_bins(self) -> torch.Tensor:
-        """``spot_bins`` random bins whose virtual crystals lie in a random pool of 48 of the 312
-        transaxial positions (all rings): the spot-check SSS then preprocesses 1,248 crystals
-        instead of 8,112 while the bins still spread over every plane, radius and 48 views."""
-        geo = self.geo
-        pos = torch.randperm(geo.vt, generator=self.gen, device=geo.device)[:48]
-        pool = torch.zeros(geo.vt * geo.vr, dtype=torch.bool, device=geo.device)
-        pool[(torch.arange(geo.vr, device=geo.device)[:, None] * geo.vt + pos[None, :]).reshape(-1)] = True
-        pr = geo.pairs_dev.long()
-        cand = torch.nonzero(pool[pr[:, 0]] & pool[pr[:, 1]]).reshape(-1)
-        pick = torch.randperm(cand.numel(), generator=self.gen, device=geo.device)[: self.spot_bins]
-        return cand.index_select(0, pick)
+    def _spot_sss(self, emission: torch.Tensor, mu: torch.Tensor):
+        """(bins, SSS of those bins) for ``spot_bins`` bins of the next pool; asynchronous."""
+        from .scatter_sinogram import sss_pairs
+        cand, local, cpos = self.pools[self.calls % self.N_POOLS]
+        self.calls += 1
+        pick = torch.randint(0, cand.numel(), (self.spot_bins,), generator=self.gen, device=cand.device)
+        return cand.index_select(0, pick), sss_pairs(self.geo, emission, mu, cpos, local.index_select(0, pick))
+
+    @staticmethod
+    def _rel(p: torch.Tensor, ref: torch.Tensor) -> torch.Tensor:
+        return torch.linalg.vector_norm(p - ref) / torch.linalg.vector_norm(ref).clamp_min(1e-30)
 
     def spot_check(self, emission: torch.Tensor, mu: torch.Tensor, pred: torch.Tensor) -> float:
-        from .scatter_sinogram import sss_sinogram
-        bins = self.draw_spot_bins()
-        ref = sss_sinogram(self.geo, emission, mu, bins=bins)
-        p = pred.index_select(0, bins)
-        return float((torch.linalg.vector_norm(p - ref) / torch.linalg.vector_norm(ref).clamp_min(1e-30)).item())
+        bins, ref = self._spot_sss(emission, mu)
+        return float(self._rel(pred.index_select(0, bins), ref).item())
 
     def estimate(self, emission: torch.Tensor, mu: torch.Tensor):
         from .scatter_sinogram import sss_sinogram
+        main = torch.cuda.current_stream(self.geo.device)
+        self.side.wait_stream(main)
+        with torch.cuda.stream(self.side):
+            bins, ref = self._spot_sss(emission, mu)
         pred = self.predict(emission, mu)
-        err = self.spot_check(emission, mu, pred)
+        main.wait_stream(self.side)
+        for t in (bins, ref):
+            t.record_stream(main)
+        err = float(self._rel(pred.index_select(0, bins), ref).item())
         if not (err <= self.fallback_tol):
             return sss_sinogram(self.geo, emission, mu), {"spot_rel_l2": err, "fallback": True}
         return pred, {"spot_rel_l2": err, "fallback": False}
@@ -336,7 +391,7 @@ def build_dataset(geo, seeds, log=None):
         inp, scale = network_input(geo, em, mu)
         X[i] = inp[0]
         T[i] = target_full(sc, scale)
-        scales[i] = scale
+        scales[i] = float(scale)
         if log and (i + 1) % 200 == 0:
             log(f"dataset {i + 1}/{n}")
     return X, T, scales
