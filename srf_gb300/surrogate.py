@@ -359,7 +359,9 @@ class ScatterSurrogate:
         bins, ref = self._spot_sss(emission, mu)
         return float(self._rel(pred.index_select(0, bins), ref).item())
 
-    def estimate(self, emission: torch.Tensor, mu: torch.Tensor):
+    def estimate(self, emission: torch.Tensor, mu: torch.Tensor, fallback: bool = True):
+        """(sinogram, record). With ``fallback=False`` the prediction is returned even when its
+        spot check failed (the record still says so)."""
         from .scatter_sinogram import sss_sinogram
         main = torch.cuda.current_stream(self.geo.device)
         self.side.wait_stream(main)
@@ -371,7 +373,9 @@ class ScatterSurrogate:
             t.record_stream(main)
         err = float(self._rel(pred.index_select(0, bins), ref).item())
         if not (err <= self.fallback_tol):
-            return sss_sinogram(self.geo, emission, mu), {"spot_rel_l2": err, "fallback": True}
+            if fallback:
+                return sss_sinogram(self.geo, emission, mu), {"spot_rel_l2": err, "fallback": True}
+            return pred, {"spot_rel_l2": err, "fallback": False, "spot_failed": True}
         return pred, {"spot_rel_l2": err, "fallback": False}
 
 
