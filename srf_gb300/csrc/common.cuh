@@ -62,12 +62,12 @@ constexpr int kBlock = 256;
 // Blocks for a grid-stride kernel over `units` work items of `per_block` items each: enough to
 // fill every SM to its occupancy limit, never more than the work needs.
 template <typename K>
-inline unsigned grid_for(K kernel, int64_t units, int per_block, int smem = 0) {
+inline unsigned grid_for(K kernel, int64_t units, int per_block, int smem = 0, int block = kBlock) {
     static thread_local int cache_dev = -1;
     int dev = 0;
     cudaGetDevice(&dev);
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kBlock, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, block, smem);
     if (occ < 1) occ = 1;
     (void)cache_dev;
     int64_t need = (units + per_block - 1) / per_block;

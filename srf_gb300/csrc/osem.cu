@@ -169,13 +169,17 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
 // One warp handles 32 consecutive LORs per round: lane j sets up LOR j into shared memory, then
 // the warp's 32/G groups walk the records. x/x_t and bp/bp_t have equal strides (offsets are
 // computed once for the gather and the scatter).
+// Single-study blocks are 128 threads: with the 4-slab variant's register budget (<= 102 per
+// thread at 5 blocks per SM) that is 20 resident warps per SM instead of 16 with 256-thread blocks.
+constexpr int kOsemBlock = 128;
+
 template <int G, bool TOF, int U, int MINB>
-__global__ void __launch_bounds__(kBlock, MINB)
+__global__ void __launch_bounds__(kOsemBlock, MINB)
 k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
               int tof_stride, Grid g, TofParams tp, const float *__restrict__ y,
               const float *__restrict__ add, int rule, float eps, View x, View xt, View bp, View bpt,
               double *__restrict__ loglik) {
-    __shared__ LorRec recs[kBlock / 32][32];
+    __shared__ LorRec recs[kOsemBlock / 32][32];
     const int wib = threadIdx.x >> 5;
     const int lane32 = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -199,8 +203,8 @@ static int launch_osem_g(const float *lors, int64_t n, int stride, const float *
                          const View &x, const View &xt, const View &bp, const View &bpt,
                          double *loglik, cudaStream_t s) {
     auto kern = k_osem_subset<G, TOF, U, MINB>;
-    unsigned blocks = grid_for(kern, n, kBlock);
-    kern<<<blocks, kBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik);
+    unsigned blocks = grid_for(kern, n, kOsemBlock, 0, kOsemBlock);
+    kern<<<blocks, kOsemBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik);
     return check_cuda("osem subset kernel launch");
 }
 
@@ -210,8 +214,8 @@ static int launch_osem_u(const float *lors, int64_t n, int stride, const float *
                          const View &x, const View &xt, const View &bp, const View &bpt,
                          double *loglik, cudaStream_t s) {
     if (slabs_per_lane() == 2)
-        return launch_osem_g<G, TOF, 2, 3>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik, s);
-    return launch_osem_g<G, TOF, 4, 2>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik, s);
+        return launch_osem_g<G, TOF, 2, 6>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik, s);
+    return launch_osem_g<G, TOF, 4, 5>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik, s);
 }
 
 template <bool TOF>
