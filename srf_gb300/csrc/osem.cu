@@ -363,12 +363,12 @@ __device__ __forceinline__ void decode_study(const srf_study &st, const TofParam
 // the next launch in stream order. The batch offsets are staged in shared memory (when they
 // fit), and a warp decodes a study descriptor only when it moves to another study.
 template <int G, bool TOF, int U, int MINB>
-__global__ void __launch_bounds__(kBlock, MINB)
+__global__ void __launch_bounds__(kOsemBlock, MINB)
 k_osem_batch(const srf_study *__restrict__ studies, int n_studies, const int64_t *__restrict__ boff,
              int64_t total_batches, TofParams tp, int rule, float eps, double *__restrict__ loglik) {
-    __shared__ LorRec recs[kBlock / 32][32];
+    __shared__ LorRec recs[kOsemBlock / 32][32];
     __shared__ int64_t soff[kMaxStudiesSmem + 1];
-    __shared__ WarpStudy wst[kBlock / 32];
+    __shared__ WarpStudy wst[kOsemBlock / 32];
     const bool staged = n_studies <= kMaxStudiesSmem;
     if (staged)
         for (int t = threadIdx.x; t <= n_studies; t += blockDim.x) soff[t] = __ldg(boff + t);
@@ -442,8 +442,8 @@ static int launch_batch_g(const srf_study *studies, int n_studies, const int64_t
                           int64_t total, const TofParams &tp, int rule, float eps, double *ll,
                           cudaStream_t s) {
     auto kern = k_osem_batch<G, TOF, U, MINB>;
-    unsigned blocks = grid_for(kern, total * 32, kBlock);
-    kern<<<blocks, kBlock, 0, s>>>(studies, n_studies, boff, total, tp, rule, eps, ll);
+    unsigned blocks = grid_for(kern, total * 32, kOsemBlock, 0, kOsemBlock);
+    kern<<<blocks, kOsemBlock, 0, s>>>(studies, n_studies, boff, total, tp, rule, eps, ll);
     return check_cuda("osem batch kernel launch");
 }
 
@@ -452,12 +452,12 @@ static int launch_batch(const srf_study *studies, int n_studies, const int64_t *
                         const TofParams &tp, int rule, float eps, double *ll, cudaStream_t s) {
     const int u = slabs_per_lane();
     switch (group_lanes()) {
-    case 8: return u == 2 ? launch_batch_g<8, TOF, 2, 3>(studies, n_studies, boff, total, tp, rule, eps, ll, s)
-                          : launch_batch_g<8, TOF, 4, 2>(studies, n_studies, boff, total, tp, rule, eps, ll, s);
-    case 16: return u == 2 ? launch_batch_g<16, TOF, 2, 3>(studies, n_studies, boff, total, tp, rule, eps, ll, s)
-                           : launch_batch_g<16, TOF, 4, 2>(studies, n_studies, boff, total, tp, rule, eps, ll, s);
-    default: return u == 2 ? launch_batch_g<32, TOF, 2, 3>(studies, n_studies, boff, total, tp, rule, eps, ll, s)
-                           : launch_batch_g<32, TOF, 4, 2>(studies, n_studies, boff, total, tp, rule, eps, ll, s);
+    case 8: return u == 2 ? launch_batch_g<8, TOF, 2, 6>(studies, n_studies, boff, total, tp, rule, eps, ll, s)
+                          : launch_batch_g<8, TOF, 4, 5>(studies, n_studies, boff, total, tp, rule, eps, ll, s);
+    case 16: return u == 2 ? launch_batch_g<16, TOF, 2, 6>(studies, n_studies, boff, total, tp, rule, eps, ll, s)
+                           : launch_batch_g<16, TOF, 4, 5>(studies, n_studies, boff, total, tp, rule, eps, ll, s);
+    default: return u == 2 ? launch_batch_g<32, TOF, 2, 6>(studies, n_studies, boff, total, tp, rule, eps, ll, s)
+                           : launch_batch_g<32, TOF, 4, 5>(studies, n_studies, boff, total, tp, rule, eps, ll, s);
     }
 }
 
