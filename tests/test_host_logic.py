@@ -154,3 +154,21 @@ def test_coarse_scatter_geometry_bins_round_trip():
         assert j >= 0
         assert any(sorted(geo.pairs[j]) == sorted(geo.pairs[k]) for k in picks[:20])
     assert hit.mean() > 0.5
+
+
+def test_surrogate_spot_pools_index_their_own_crystals():
+    """The spot-check pools (built once on the host) list bins whose two virtual crystals lie in
+    the pool, with indices into the pool's crystal positions that name the same crystals."""
+    import types
+    from srf_gb300 import synth
+    from srf_gb300.scatter_sinogram import CoarseGeometry
+    from srf_gb300.surrogate import ScatterSurrogate
+    geo = CoarseGeometry(synth.scanner_clinical(), device="cpu")
+    fake = types.SimpleNamespace(geo=geo, N_POOLS=3, POOL_POSITIONS=48)
+    pools = ScatterSurrogate._make_pools(fake, 5)
+    assert len(pools) == 3
+    for cand, local, cpos in pools:
+        assert cpos.shape == (48 * geo.vr, 3) and cand.numel() > 2048
+        pr = geo.pairs[cand.numpy()]
+        for col in range(2):
+            assert np.array_equal(geo.vpos[pr[:, col]], cpos.numpy()[local[:, col].numpy()])
