@@ -361,4 +361,14 @@ __device__ __forceinline__ void candidates_exact(const LorRun &r, const GridK &k
     slab_voxels(r, ip, keep, qq1, qq2, zz1, zz2, r.wc * w_tof, o, w);
 }
 
+// The standalone projector / backprojector on the fused kernel's traversal (osem.cu). tof == NULL
+// selects the non-TOF rules. Views with equal strides for the two layouts (v x-fastest, vt the
+// optional y-fastest copy).
+int fused_projection(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                     const Grid &g, const TofParams &tp, const View &v, const View &vt, float *out,
+                     cudaStream_t s);
+int fused_backprojection(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                         const Grid &g, const TofParams &tp, const float *values, const View &v,
+                         const View &vt, cudaStream_t s);
+
 }  // namespace srf

@@ -15,10 +15,8 @@ namespace srf {
 // Generic path for a LOR whose projector and backprojector traverse along different axes
 // (non-TOF with |xd| == |yd|): two setups, as in the standalone kernels.
 template <int G, bool TOF>
-__device__ __forceinline__ void tie_path(const float *l, float tv, float yv, float ad, int lane, const Grid &g,
-                                         const TofParams &tp, const View &x, const View &xt,
-                                         const View &bp, const View &bpt, int rule, float eps,
-                                         double &ll, bool want_ll) {
+__device__ __forceinline__ float tie_project(const float *l, float tv, int lane, const Grid &g, const TofParams &tp,
+                                             const View &x, const View &xt) {
     float acc = 0.0f;
     LorSetup S;
     if (setup_lor<TOF, RULES_PROJ>(l[0], l[1], l[2], l[3], l[4], l[5], tv, g, tp, x.st, xt.st, xt.ptr != nullptr, S)) {
@@ -26,15 +24,30 @@ __device__ __forceinline__ void tie_path(const float *l, float tv, float yv, flo
         for (int ip = S.lo + lane; ip <= S.hi; ip += G)
             slab<TOF, RULES_PROJ>(S, ip, [&](int32_t off, float w) { acc += __ldg(im + off) * w; });
     }
-    const float p = group_sum<G>(acc);
-    const float den = __fadd_rn(__fadd_rn(p, ad), eps);
-    const float r = (rule == SRF_RATIO_DIV_NO_NAN) ? ((den == 0.0f) ? 0.0f : __fdiv_rn(yv, den)) : __fdiv_rn(yv, den);
-    if (want_ll && lane == 0 && den > 0.0f) ll += (double)yv * (double)__logf(den);
+    return group_sum<G>(acc);
+}
+
+template <int G, bool TOF>
+__device__ __forceinline__ void tie_backproject(const float *l, float tv, float r, int lane, const Grid &g,
+                                                const TofParams &tp, const View &bp, const View &bpt) {
+    LorSetup S;
     if (r != 0.0f && setup_lor<TOF, RULES_BACK>(l[0], l[1], l[2], l[3], l[4], l[5], tv, g, tp, bp.st, bpt.st, bpt.ptr != nullptr, S)) {
         float *im = (!S.xdom && bpt.ptr) ? bpt.ptr : bp.ptr;
         for (int ip = S.lo + lane; ip <= S.hi; ip += G)
             slab<TOF, RULES_BACK>(S, ip, [&](int32_t off, float w) { atomicAdd(im + off, r * w); });
     }
+}
+
+template <int G, bool TOF>
+__device__ __forceinline__ void tie_path(const float *l, float tv, float yv, float ad, int lane, const Grid &g,
+                                         const TofParams &tp, const View &x, const View &xt,
+                                         const View &bp, const View &bpt, int rule, float eps,
+                                         double &ll, bool want_ll) {
+    const float p = tie_project<G, TOF>(l, tv, lane, g, tp, x, xt);
+    const float den = __fadd_rn(__fadd_rn(p, ad), eps);
+    const float r = (rule == SRF_RATIO_DIV_NO_NAN) ? ((den == 0.0f) ? 0.0f : __fdiv_rn(yv, den)) : __fdiv_rn(yv, den);
+    if (want_ll && lane == 0 && den > 0.0f) ll += (double)yv * (double)__logf(den);
+    tie_backproject<G, TOF>(l, tv, r, lane, g, tp, bp, bpt);
 }
 
 // U slabs of one chunk per lane: fast candidates for all (independent, so they interleave), then
@@ -62,10 +75,14 @@ __device__ __forceinline__ void chunk_candidates(const LorRun &run, const GridK 
         if (bad[u]) candidates_exact<TOF>(run, k, c0 + lane + G * u, o[u], w[u], pm[u]);
 }
 
+// What a traversal of osem_warp_batch does per LOR: the fused OSEM step, or one of its two halves
+// on its own (the projector into out[i], or the backprojector of the values passed as y).
+enum TraceMode : int { MODE_FUSED = 0, MODE_PROJ = 1, MODE_BACK = 2 };
+
 // LORs [base, base + 32) of one study: lane-parallel setup of the 32 records into wrecs, then
 // the warp's 32/G groups walk them (projection, ratio, backprojection per LOR). x/x_t and
 // bp/bp_t have equal strides (offsets are computed once for the gather and the scatter).
-template <int G, bool TOF, int U>
+template <int G, bool TOF, int U, int MODE = MODE_FUSED>
 __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__restrict__ lors,
                                                 int64_t n, int stride, const float *__restrict__ tof,
                                                 int tof_stride, const Grid &g, const GridK &k,
@@ -73,7 +90,7 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
                                                 const float *__restrict__ add, int rule, float eps,
                                                 const View &x, const View &xt,
                                                 const View &bp, const View &bpt, int64_t base,
-                                                bool want_ll, double &ll) {
+                                                bool want_ll, double &ll, float *__restrict__ out = nullptr) {
     constexpr int GPW = 32 / G;
     const int lane32 = threadIdx.x & 31;
     const int lane = threadIdx.x & (G - 1);
@@ -106,7 +123,14 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
 #pragma unroll
             for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
             const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
-            tie_path<G, TOF>(lv, tv, R.yv, R.ad, lane, g, tp, x, xt, bp, bpt, rule, eps, ll, want_ll);
+            if (MODE == MODE_FUSED) {
+                tie_path<G, TOF>(lv, tv, R.yv, R.ad, lane, g, tp, x, xt, bp, bpt, rule, eps, ll, want_ll);
+            } else if (MODE == MODE_PROJ) {
+                const float p = tie_project<G, TOF>(lv, tv, lane, g, tp, x, xt);
+                if (lane == 0) out[i] = p;
+            } else {
+                tie_backproject<G, TOF>(lv, tv, R.yv, lane, g, tp, bp, bpt);
+            }
             continue;
         }
         const bool valid = R.flags & F_VALID;
@@ -119,7 +143,7 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
         float w[U][3];
         bool pm[U];
         float acc = 0.0f;
-        if (valid) {
+        if (MODE != MODE_BACK && valid) {
             for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
                 chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
                 if (proj_ok) {
@@ -136,17 +160,26 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
                 }
             }
         }
-        const float p = group_sum<G>(acc) * R.invL2;
-        if (!valid) continue;
-        const float den = __fadd_rn(__fadd_rn(p, R.ad), eps);
         float r;
-        if (rule == SRF_RATIO_DIV_NO_NAN)
-            r = (den == 0.0f) ? 0.0f : __fdiv_rn(R.yv, den);
-        else
-            r = __fdiv_rn(R.yv, den);
-        if (want_ll && lane == 0 && den > 0.0f) ll += (double)R.yv * (double)__logf(den);
+        if (MODE == MODE_BACK) {
+            if (!valid) continue;
+            r = R.yv;
+        } else {
+            const float p = group_sum<G>(acc) * R.invL2;
+            if (MODE == MODE_PROJ) {
+                if (lane == 0 && i < n) out[i] = p;  // 0 for a skipped LOR, as the reference's memset
+                continue;
+            }
+            if (!valid) continue;
+            const float den = __fadd_rn(__fadd_rn(p, R.ad), eps);
+            if (rule == SRF_RATIO_DIV_NO_NAN)
+                r = (den == 0.0f) ? 0.0f : __fdiv_rn(R.yv, den);
+            else
+                r = __fdiv_rn(R.yv, den);
+            if (want_ll && lane == 0 && den > 0.0f) ll += (double)R.yv * (double)__logf(den);
+        }
         if (r == 0.0f) continue;
-        if (single) {
+        if (MODE == MODE_FUSED && single) {
 #pragma unroll
             for (int u = 0; u < U; ++u)
 #pragma unroll
@@ -195,6 +228,61 @@ k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float
         for (int o2 = 16; o2 > 0; o2 >>= 1) ll += __shfl_xor_sync(0xffffffffu, ll, o2);
         if (lane32 == 0 && ll != 0.0) atomicAdd(loglik, ll);
     }
+}
+
+// The standalone projector (MODE_PROJ: out[i] for every LOR of x / x_t) and backprojector
+// (MODE_BACK: values[i] into the accumulators bp / bp_t) on the fused kernel's traversal, for
+// srf_projection(_tof) and srf_backprojection(_tof).
+template <int G, bool TOF, int U, int MINB, int MODE>
+__global__ void __launch_bounds__(kOsemBlock, MINB)
+k_trace_fused(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
+              int tof_stride, Grid g, TofParams tp, const float *__restrict__ values, float *__restrict__ out,
+              View v, View vt) {
+    __shared__ LorRec recs[kOsemBlock / 32][32];
+    const int wib = threadIdx.x >> 5;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const GridK k = make_gridk<TOF>(g, tp);
+    double ll = 0.0;
+    for (int64_t base = warp * 32; base < n; base += nwarps * 32)
+        osem_warp_batch<G, TOF, U, MODE>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, values, nullptr,
+                                         SRF_RATIO_PLAIN, 0.0f, v, vt, v, vt, base, false, ll, out);
+}
+
+template <int G, bool TOF, int MODE>
+static int launch_trace_fused_g(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                                const Grid &g, const TofParams &tp, const float *values, float *out,
+                                const View &v, const View &vt, cudaStream_t s) {
+    auto kern = k_trace_fused<G, TOF, 4, 5, MODE>;
+    unsigned blocks = grid_for(kern, n, kOsemBlock, 0, kOsemBlock);
+    kern<<<blocks, kOsemBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, values, out, v, vt);
+    return check_cuda("fused trace kernel launch");
+}
+
+template <bool TOF, int MODE>
+static int launch_trace_fused(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                              const Grid &g, const TofParams &tp, const float *values, float *out,
+                              const View &v, const View &vt, cudaStream_t s) {
+    if (n == 0) return ok();
+    switch (group_lanes()) {
+    case 8: return launch_trace_fused_g<8, TOF, MODE>(lors, n, stride, tof, tof_stride, g, tp, values, out, v, vt, s);
+    case 16: return launch_trace_fused_g<16, TOF, MODE>(lors, n, stride, tof, tof_stride, g, tp, values, out, v, vt, s);
+    default: return launch_trace_fused_g<32, TOF, MODE>(lors, n, stride, tof, tof_stride, g, tp, values, out, v, vt, s);
+    }
+}
+
+int fused_projection(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                     const Grid &g, const TofParams &tp, const View &v, const View &vt, float *out,
+                     cudaStream_t s) {
+    return tof ? launch_trace_fused<true, MODE_PROJ>(lors, n, stride, tof, tof_stride, g, tp, nullptr, out, v, vt, s)
+               : launch_trace_fused<false, MODE_PROJ>(lors, n, stride, nullptr, 1, g, tp, nullptr, out, v, vt, s);
+}
+
+int fused_backprojection(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                         const Grid &g, const TofParams &tp, const float *values, const View &v,
+                         const View &vt, cudaStream_t s) {
+    return tof ? launch_trace_fused<true, MODE_BACK>(lors, n, stride, tof, tof_stride, g, tp, values, nullptr, v, vt, s)
+               : launch_trace_fused<false, MODE_BACK>(lors, n, stride, nullptr, 1, g, tp, values, nullptr, v, vt, s);
 }
 
 template <int G, bool TOF, int U, int MINB>

@@ -1,6 +1,7 @@
 // Projector family: forward projection, backprojection, exact adjoint (non-TOF and TOF), and the
 // view fold/copy helpers. Kernels are grid-stride over LORs, G lanes per LOR (siddon.cuh).
 #include "common.cuh"
+#include "fused.cuh"
 
 namespace srf {
 
@@ -244,7 +245,7 @@ int srf_projection(const float *lors, int64_t n, int32_t lor_stride, const float
     if ((rc = common_args(lors, n, lor_stride, image, image_strides, image_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
     if (n > 0 && !out) return fail(SRF_EINVAL, "out must not be NULL");
     TofParams tp{0, 0, 0};
-    return launch_trace<false, RULES_PROJ, GATHER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, nullptr, out, (cudaStream_t)stream);
+    return fused_projection(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, out, (cudaStream_t)stream);
 }
 
 int srf_backprojection(const float *lors, int64_t n, int32_t lor_stride, const float *values,
@@ -255,7 +256,7 @@ int srf_backprojection(const float *lors, int64_t n, int32_t lor_stride, const f
     if ((rc = common_args(lors, n, lor_stride, image, image_strides, image_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
     if (n > 0 && !values) return fail(SRF_EINVAL, "values must not be NULL");
     TofParams tp{0, 0, 0};
-    return launch_trace<false, RULES_BACK, SCATTER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
+    return fused_backprojection(lors, n, lor_stride, nullptr, 1, g, tp, values, v, vt, (cudaStream_t)stream);
 }
 
 int srf_projection_tof(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
@@ -267,7 +268,7 @@ int srf_projection_tof(const float *lors, int64_t n, int32_t lor_stride, const f
     if ((rc = common_args(lors, n, lor_stride, image, image_strides, image_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
     if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
     if (n > 0 && !out) return fail(SRF_EINVAL, "out must not be NULL");
-    return launch_trace<true, RULES_PROJ, GATHER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, nullptr, out, (cudaStream_t)stream);
+    return fused_projection(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, out, (cudaStream_t)stream);
 }
 
 int srf_backprojection_tof(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
@@ -280,7 +281,7 @@ int srf_backprojection_tof(const float *lors, int64_t n, int32_t lor_stride, con
     if ((rc = common_args(lors, n, lor_stride, image, image_strides, image_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
     if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
     if (n > 0 && !values) return fail(SRF_EINVAL, "values must not be NULL");
-    return launch_trace<true, RULES_BACK, SCATTER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
+    return fused_backprojection(lors, n, lor_stride, tof, tof_stride, g, tp, values, v, vt, (cudaStream_t)stream);
 }
 
 int srf_projection_adjoint(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
