@@ -1,11 +1,13 @@
-// Projector family: forward projection, backprojection, exact adjoint (non-TOF and TOF), and the
-// view fold/copy helpers. Kernels are grid-stride over LORs, G lanes per LOR (siddon.cuh).
+// Projector family entry points: forward projection and backprojection (non-TOF and TOF; these run
+// on the fused kernel's traversal in osem.cu), the exact adjoint, visit counts, attenuation, the
+// batched projector, and the view fold/copy helpers. k_trace here is grid-stride over LORs with G
+// lanes per LOR and the per-slab setup of siddon.cuh.
 #include "common.cuh"
 #include "fused.cuh"
 
 namespace srf {
 
-enum Action : int { GATHER = 0, SCATTER = 1, COUNT = 2, ATTEN = 3 };
+enum Action : int { GATHER = 0, SCATTER = 1, COUNT = 2 };  // GATHER: k_trace_batch only
 
 // Warp-uniform loop over LORs: each warp takes 32/G consecutive LORs per round, so the group
 // shuffles in group_sum always see all 32 lanes.
@@ -35,10 +37,6 @@ k_trace(const float *__restrict__ lors, int64_t n, int stride, const float *__re
                 if (ACTION == COUNT) {
                     for (int ip = S.lo + lane; ip <= S.hi; ip += G)
                         slab<TOF, RULES>(S, ip, [&](int32_t, float) { acc += 1.0f; });
-                } else if (ACTION == GATHER || ACTION == ATTEN) {
-                    const float *imc = im;
-                    for (int ip = S.lo + lane; ip <= S.hi; ip += G)
-                        slab<TOF, RULES>(S, ip, [&](int32_t off, float w) { acc += __ldg(imc + off) * w; });
                 } else {
                     const float val = __ldg(values + i);
                     if (val != 0.0f)
@@ -47,23 +45,7 @@ k_trace(const float *__restrict__ lors, int64_t n, int stride, const float *__re
                 }
             }
         }
-        if (ACTION == GATHER) {
-            acc = group_sum<G>(acc);
-            if (valid && lane == 0) out[i] = acc;
-        } else if (ACTION == ATTEN) {
-            // UmapProject epilogue: exp(-(p * L * L / unit)), L from the raw endpoints in FP32
-            acc = group_sum<G>(acc);
-            if (valid && lane == 0) {
-                const float *l = lors + i * stride;
-                const float dx = __fsub_rn(__ldg(l), __ldg(l + 3)), dy = __fsub_rn(__ldg(l + 1), __ldg(l + 4));
-                const float dz = __fsub_rn(__ldg(l + 2), __ldg(l + 5));
-                const float L = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-                const float unit = __fdiv_rn(g.sx, (float)g.nx);
-                const float v = __fdiv_rn(__fmul_rn(__fmul_rn(acc, L), L), unit);
-                const float a = expf(-v);
-                out[i] = values ? __fdiv_rn(__ldg(values + i), a) : a;
-            }
-        } else if (ACTION == COUNT) {
+        if (ACTION == COUNT) {
             acc = group_sum<G>(acc);  // < 2^24 visits per LOR, exact in FP32
             if (valid && lane == 0 && acc > 0.0f)
                 atomicAdd((unsigned long long *)out, (unsigned long long)acc);
@@ -179,6 +161,23 @@ static int launch_batch_trace(const float *lors, int64_t n, int stride, const fl
     case 8: return launch_batch_trace_g<8, TOF, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride, s);
     case 16: return launch_batch_trace_g<16, TOF, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride, s);
     default: return launch_batch_trace_g<32, TOF, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride, s);
+    }
+}
+
+// UmapProject's epilogue over projections already in out (attenuation_correct.py:34-40):
+// a = exp(-(p * L * L / unit)) with L from the raw endpoints in FP32; out = values / a when values
+// are given (AttenuationCorrect), else a.
+__global__ void k_atten_epilogue(const float *__restrict__ lors, int64_t n, int stride, Grid g,
+                                 const float *__restrict__ values, float *__restrict__ out) {
+    const float unit = __fdiv_rn(g.sx, (float)g.nx);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float *l = lors + i * stride;
+        const float dx = __fsub_rn(__ldg(l), __ldg(l + 3)), dy = __fsub_rn(__ldg(l + 1), __ldg(l + 4));
+        const float dz = __fsub_rn(__ldg(l + 2), __ldg(l + 5));
+        const float L = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+        const float v = __fdiv_rn(__fmul_rn(__fmul_rn(out[i], L), L), unit);
+        const float a = expf(-v);
+        out[i] = values ? __fdiv_rn(__ldg(values + i), a) : a;
     }
 }
 
@@ -391,7 +390,11 @@ int srf_attenuation(const float *lors, int64_t n, int32_t lor_stride, const floa
     if ((rc = common_args(lors, n, lor_stride, umap, umap_strides, nullptr, nullptr, grid, center, size, g, v, vt))) return rc;
     if (n > 0 && !out) return fail(SRF_EINVAL, "out must not be NULL");
     TofParams tp{0, 0, 0};
-    return launch_trace<false, RULES_PROJ, ATTEN>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, values, out, (cudaStream_t)stream);
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc2 = fused_projection(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, out, s);
+    if (rc2 || n == 0) return rc2;
+    k_atten_epilogue<<<grid_for(k_atten_epilogue, n, 256), 256, 0, s>>>(lors, n, lor_stride, g, values, out);
+    return check_cuda("attenuation epilogue launch");
 }
 
 static int elementwise_args(const void *dst, const int64_t *ds, const void *src, const int64_t *ss,

@@ -270,8 +270,8 @@ __device__ __forceinline__ void slab(const LorSetup &S, int ip, F &&visit) {
 // Lanes of this thread's group of G (G a power of two <= 32, groups aligned within the warp).
 template <int G>
 __device__ __forceinline__ unsigned group_mask() {
-    if (G == 32) return 0xffffffffu;
-    return ((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1));
+    if constexpr (G == 32) return 0xffffffffu;
+    else return ((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1));
 }
 
 // Sum over a group of G lanes. Only the group's own lanes take part, so groups of one warp may
