@@ -370,5 +370,12 @@ int fused_projection(const float *lors, int64_t n, int stride, const float *tof,
 int fused_backprojection(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
                          const Grid &g, const TofParams &tp, const float *values, const View &v,
                          const View &vt, cudaStream_t s);
+// The projector and its exact adjoint for nb <= 8 images at element offsets b * bstride.
+int fused_projection_batch(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                           const Grid &g, const TofParams &tp, int nb, int64_t bstride, const View &v,
+                           const View &vt, float *out, int64_t ostride, cudaStream_t s);
+int fused_adjoint_batch(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                        const Grid &g, const TofParams &tp, int nb, int64_t bstride, const float *values,
+                        int64_t vstride, const View &v, const View &vt, cudaStream_t s);
 
 }  // namespace srf

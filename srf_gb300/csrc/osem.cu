@@ -77,7 +77,7 @@ __device__ __forceinline__ void chunk_candidates(const LorRun &run, const GridK 
 
 // What a traversal of osem_warp_batch does per LOR: the fused OSEM step, or one of its two halves
 // on its own (the projector into out[i], or the backprojector of the values passed as y).
-enum TraceMode : int { MODE_FUSED = 0, MODE_PROJ = 1, MODE_BACK = 2 };
+enum TraceMode : int { MODE_FUSED = 0, MODE_PROJ = 1, MODE_BACK = 2, MODE_ADJ = 3 };
 
 // LORs [base, base + 32) of one study: lane-parallel setup of the 32 records into wrecs, then
 // the warp's 32/G groups walk them (projection, ratio, backprojection per LOR). x/x_t and
@@ -283,6 +283,153 @@ int fused_backprojection(const float *lors, int64_t n, int stride, const float *
                          const View &vt, cudaStream_t s) {
     return tof ? launch_trace_fused<true, MODE_BACK>(lors, n, stride, tof, tof_stride, g, tp, values, nullptr, v, vt, s)
                : launch_trace_fused<false, MODE_BACK>(lors, n, stride, nullptr, 1, g, tp, values, nullptr, v, vt, s);
+}
+
+// ---------------------------------------------------------------- batched projector / adjoint
+// The projector (MODE_PROJ) and its exact adjoint (MODE_ADJ: projector rules, projector weights
+// with 1/L^2, scattered) for nb <= kMaxBatch images that share the grid and the LORs: image b at
+// element offset b * bstride in both layouts; values / out are nb rows of n at row stride ostride.
+// Each LOR is set up once and its slab candidates are computed once for all images.
+constexpr int kMaxBatch = 8;
+
+template <int G, bool TOF, int MODE>
+__device__ __forceinline__ void tie_batch(const float *l, float tv, int lane, const Grid &g, const TofParams &tp,
+                                          const View &v, const View &vt, int nb, int64_t bstride,
+                                          const float (&val)[kMaxBatch], float (&acc)[kMaxBatch]) {
+    LorSetup S;
+    if (!setup_lor<TOF, RULES_PROJ>(l[0], l[1], l[2], l[3], l[4], l[5], tv, g, tp, v.st, vt.st, vt.ptr != nullptr, S)) return;
+    float *im = (!S.xdom && vt.ptr) ? vt.ptr : v.ptr;
+    for (int ip = S.lo + lane; ip <= S.hi; ip += G)
+        slab<TOF, RULES_PROJ>(S, ip, [&](int32_t off, float w) {
+#pragma unroll
+            for (int b = 0; b < kMaxBatch; ++b) {
+                if (b >= nb) continue;
+                if (MODE == MODE_PROJ) acc[b] = fmaf(__ldg(im + b * bstride + off), w, acc[b]);
+                else if (val[b] != 0.0f) atomicAdd(im + b * bstride + off, val[b] * w);
+            }
+        });
+}
+
+template <int G, bool TOF, int U, int MODE>
+__device__ __forceinline__ void batch_warp(LorRec *wrecs, const float *__restrict__ lors, int64_t n, int stride,
+                                           const float *__restrict__ tof, int tof_stride, const Grid &g,
+                                           const GridK &k, const TofParams &tp, int nb, int64_t bstride,
+                                           const float *__restrict__ values, float *__restrict__ out,
+                                           int64_t ostride, const View &v, const View &vt, int64_t base) {
+    constexpr int GPW = 32 / G;
+    const int lane32 = threadIdx.x & 31;
+    const int lane = threadIdx.x & (G - 1);
+    const int gi = lane32 / G;
+    const bool have_t = vt.ptr != nullptr;
+    {
+        const int64_t i = base + lane32;
+        LorRec R = {};
+        R.lo = 1;
+        if (i < n) {
+            const float *l = lors + i * stride;
+            float lv[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
+            const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
+            R = setup_rec<TOF>(lv, tv, 1.0f, g, k);
+        }
+        store_rec(&wrecs[lane32], R);
+    }
+    __syncwarp();
+    for (int j0 = 0; j0 < 32; j0 += GPW) {
+        const int j = j0 + gi;
+        const LorRec R = load_rec(&wrecs[j]);
+        const int64_t i = base + j;
+        float acc[kMaxBatch], val[kMaxBatch];
+        bool any = false;
+#pragma unroll
+        for (int b = 0; b < kMaxBatch; ++b) {
+            acc[b] = 0.0f;
+            val[b] = (MODE == MODE_ADJ && b < nb && i < n) ? __ldg(values + b * ostride + i) : 0.0f;
+            any = any || val[b] != 0.0f;
+        }
+        if (!TOF && (R.flags & F_TIE)) {  // ties exist only under the non-TOF projector rule
+            float lv[6];
+            const float *l = lors + i * stride;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
+            if (MODE == MODE_PROJ || any) tie_batch<G, TOF, MODE>(lv, 0.0f, lane, g, tp, v, vt, nb, bstride, val, acc);
+        } else if ((R.flags & F_VALID) && (R.flags & F_PROJ) && (MODE == MODE_PROJ || any)) {
+            const LorRun run = make_run(R, g, k, v.st, vt.st, have_t);
+            float *im = (!run.xdom && have_t) ? vt.ptr : v.ptr;
+            if (MODE == MODE_ADJ)
+#pragma unroll
+                for (int b = 0; b < kMaxBatch; ++b) val[b] *= R.invL2;
+            int32_t o[U][3];
+            float w[U][3];
+            bool pm[U];
+            for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
+                chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        if (!(pm[u] && w[u][c] != 0.0f)) continue;
+#pragma unroll
+                        for (int b = 0; b < kMaxBatch; ++b) {
+                            if (b >= nb) continue;
+                            if (MODE == MODE_PROJ) acc[b] = fmaf(__ldg(im + b * bstride + o[u][c]), w[u][c], acc[b]);
+                            else if (val[b] != 0.0f) atomicAdd(im + b * bstride + o[u][c], val[b] * w[u][c]);
+                        }
+                    }
+            }
+#pragma unroll
+            for (int b = 0; b < kMaxBatch; ++b) acc[b] *= R.invL2;
+        }
+        if (MODE == MODE_PROJ) {
+#pragma unroll
+            for (int b = 0; b < kMaxBatch; ++b) {
+                const float p = group_sum<G>(acc[b]);
+                if (lane == 0 && i < n && b < nb) out[b * ostride + i] = p;
+            }
+        }
+    }
+    __syncwarp();
+}
+
+template <int G, bool TOF, int U, int MINB, int MODE>
+__global__ void __launch_bounds__(kOsemBlock, MINB)
+k_trace_fused_batch(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
+                    int tof_stride, Grid g, TofParams tp, int nb, int64_t bstride,
+                    const float *__restrict__ values, float *__restrict__ out, int64_t ostride, View v, View vt) {
+    __shared__ LorRec recs[kOsemBlock / 32][32];
+    const int wib = threadIdx.x >> 5;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const GridK k = make_gridk<TOF>(g, tp);
+    for (int64_t base = warp * 32; base < n; base += nwarps * 32)
+        batch_warp<G, TOF, U, MODE>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, nb, bstride, values,
+                                    out, ostride, v, vt, base);
+}
+
+template <bool TOF, int MODE>
+static int launch_fused_batch(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                              const Grid &g, const TofParams &tp, int nb, int64_t bstride, const float *values,
+                              float *out, int64_t ostride, const View &v, const View &vt, cudaStream_t s) {
+    if (n == 0) return ok();
+    auto kern = k_trace_fused_batch<32, TOF, 4, 4, MODE>;
+    unsigned blocks = grid_for(kern, n, kOsemBlock, 0, kOsemBlock);
+    kern<<<blocks, kOsemBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, nb, bstride, values, out, ostride, v, vt);
+    return check_cuda("batched projector kernel launch");
+}
+
+int fused_projection_batch(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                           const Grid &g, const TofParams &tp, int nb, int64_t bstride, const View &v,
+                           const View &vt, float *out, int64_t ostride, cudaStream_t s) {
+    return tof ? launch_fused_batch<true, MODE_PROJ>(lors, n, stride, tof, tof_stride, g, tp, nb, bstride, nullptr, out, ostride, v, vt, s)
+               : launch_fused_batch<false, MODE_PROJ>(lors, n, stride, nullptr, 1, g, tp, nb, bstride, nullptr, out, ostride, v, vt, s);
+}
+
+int fused_adjoint_batch(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
+                        const Grid &g, const TofParams &tp, int nb, int64_t bstride, const float *values,
+                        int64_t vstride, const View &v, const View &vt, cudaStream_t s) {
+    return tof ? launch_fused_batch<true, MODE_ADJ>(lors, n, stride, tof, tof_stride, g, tp, nb, bstride, values, nullptr, vstride, v, vt, s)
+               : launch_fused_batch<false, MODE_ADJ>(lors, n, stride, nullptr, 1, g, tp, nb, bstride, values, nullptr, vstride, v, vt, s);
 }
 
 template <int G, bool TOF, int U, int MINB>

@@ -7,7 +7,7 @@
 
 namespace srf {
 
-enum Action : int { GATHER = 0, SCATTER = 1, COUNT = 2 };  // GATHER: k_trace_batch only
+enum Action : int { SCATTER = 1, COUNT = 2 };
 
 // Warp-uniform loop over LORs: each warp takes 32/G consecutive LORs per round, so the group
 // shuffles in group_sum always see all 32 lanes.
@@ -75,94 +75,7 @@ static int launch_trace(const float *lors, int64_t n, int stride, const float *t
     }
 }
 
-// Projector and its exact adjoint for a batch of nb <= kMaxBatch images sharing one grid and one
-// set of LORs (image b at offset b * bstride): every LOR is set up and traversed once, and each
-// visit gathers from (or scatters into) all images. out / values hold nb rows of n at row stride
-// ostride.
-constexpr int kMaxBatch = 8;
-
-template <int G, bool TOF, int ACTION>
-__global__ void __launch_bounds__(kBlock)
-k_trace_batch(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
-              int tof_stride, Grid g, TofParams tp, View v, View vt, int nb, int64_t bstride,
-              const float *__restrict__ values, float *__restrict__ out, int64_t ostride) {
-    constexpr int GPW = 32 / G;
-    const int lane = threadIdx.x & (G - 1);
-    const int gi = (threadIdx.x & 31) / G;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const bool have_t = vt.ptr != nullptr;
-    for (int64_t base = warp * GPW; base < n; base += nwarps * GPW) {
-        const int64_t i = base + gi;
-        const bool valid = i < n;
-        float acc[kMaxBatch];
-#pragma unroll
-        for (int b = 0; b < kMaxBatch; ++b) acc[b] = 0.0f;
-        if (valid) {
-            const float *l = lors + i * stride;
-            const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
-            LorSetup S;
-            if (setup_lor<TOF, RULES_PROJ>(__ldg(l), __ldg(l + 1), __ldg(l + 2), __ldg(l + 3),
-                                           __ldg(l + 4), __ldg(l + 5), tv, g, tp, v.st, vt.st, have_t, S)) {
-                float *im = (!S.xdom && have_t) ? vt.ptr : v.ptr;
-                if (ACTION == GATHER) {
-                    const float *imc = im;
-                    for (int ip = S.lo + lane; ip <= S.hi; ip += G)
-                        slab<TOF, RULES_PROJ>(S, ip, [&](int32_t off, float w) {
-#pragma unroll
-                            for (int b = 0; b < kMaxBatch; ++b)
-                                if (b < nb) acc[b] = fmaf(__ldg(imc + b * bstride + off), w, acc[b]);
-                        });
-                } else {
-                    float val[kMaxBatch];
-                    bool any = false;
-#pragma unroll
-                    for (int b = 0; b < kMaxBatch; ++b) {
-                        val[b] = b < nb ? __ldg(values + b * ostride + i) : 0.0f;
-                        any = any || val[b] != 0.0f;
-                    }
-                    if (any)
-                        for (int ip = S.lo + lane; ip <= S.hi; ip += G)
-                            slab<TOF, RULES_PROJ>(S, ip, [&](int32_t off, float w) {
-#pragma unroll
-                                for (int b = 0; b < kMaxBatch; ++b)
-                                    if (b < nb && val[b] != 0.0f) atomicAdd(im + b * bstride + off, val[b] * w);
-                            });
-                }
-            }
-        }
-        if (ACTION == GATHER) {
-#pragma unroll
-            for (int b = 0; b < kMaxBatch; ++b) {
-                const float r = group_sum<G>(acc[b]);
-                if (valid && lane == 0 && b < nb) out[b * ostride + i] = r;
-            }
-        }
-    }
-}
-
-template <int G, bool TOF, int ACTION>
-static int launch_batch_trace_g(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
-                                const Grid &g, const TofParams &tp, const View &v, const View &vt, int nb,
-                                int64_t bstride, const float *values, float *out, int64_t ostride,
-                                cudaStream_t s) {
-    auto kern = k_trace_batch<G, TOF, ACTION>;
-    unsigned blocks = grid_for(kern, n, kBlock / G);
-    kern<<<blocks, kBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride);
-    return check_cuda("batched trace kernel launch");
-}
-
-template <bool TOF, int ACTION>
-static int launch_batch_trace(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
-                              const Grid &g, const TofParams &tp, const View &v, const View &vt, int nb,
-                              int64_t bstride, const float *values, float *out, int64_t ostride, cudaStream_t s) {
-    if (n == 0) return ok();
-    switch (group_lanes()) {
-    case 8: return launch_batch_trace_g<8, TOF, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride, s);
-    case 16: return launch_batch_trace_g<16, TOF, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride, s);
-    default: return launch_batch_trace_g<32, TOF, ACTION>(lors, n, stride, tof, tof_stride, g, tp, v, vt, nb, bstride, values, out, ostride, s);
-    }
-}
+constexpr int kMaxBatch = 8;  // images per batched projector call (as the kernel in osem.cu)
 
 // UmapProject's epilogue over projections already in out (attenuation_correct.py:34-40):
 // a = exp(-(p * L * L / unit)) with L from the raw endpoints in FP32; out = values / a when values
@@ -331,10 +244,10 @@ int srf_projection_batch(const float *lors, int64_t n, int32_t lor_stride, const
     if (tof) {
         TofParams tp;
         if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
-        return launch_batch_trace<true, GATHER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, n_images, batch_stride, nullptr, out, out_stride, s);
+        return fused_projection_batch(lors, n, lor_stride, tof, tof_stride, g, tp, n_images, batch_stride, v, vt, out, out_stride, s);
     }
     TofParams tp{0, 0, 0};
-    return launch_batch_trace<false, GATHER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, n_images, batch_stride, nullptr, out, out_stride, s);
+    return fused_projection_batch(lors, n, lor_stride, nullptr, 1, g, tp, n_images, batch_stride, v, vt, out, out_stride, s);
 }
 
 int srf_projection_adjoint_batch(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
@@ -351,10 +264,10 @@ int srf_projection_adjoint_batch(const float *lors, int64_t n, int32_t lor_strid
     if (tof) {
         TofParams tp;
         if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
-        return launch_batch_trace<true, SCATTER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, n_images, batch_stride, values, nullptr, values_stride, s);
+        return fused_adjoint_batch(lors, n, lor_stride, tof, tof_stride, g, tp, n_images, batch_stride, values, values_stride, v, vt, s);
     }
     TofParams tp{0, 0, 0};
-    return launch_batch_trace<false, SCATTER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, n_images, batch_stride, values, nullptr, values_stride, s);
+    return fused_adjoint_batch(lors, n, lor_stride, nullptr, 1, g, tp, n_images, batch_stride, values, values_stride, v, vt, s);
 }
 
 int srf_count_pairs(const float *lors, int64_t n, int32_t lor_stride, const float *tof,
