@@ -287,7 +287,7 @@ class ScatterSurrogate:
         self.side = torch.cuda.Stream(geo.device)
         self.pools = self._make_pools(seed)
         self.calls = 0
-        self._graph = self._graph_in = self._graph_out = None
+        self._graph = self._graph_out = self._em_in = self._mu_in = None
 
     def _make_pools(self, seed: int):
         """Spot-check pools, built once: each is a random set of 48 of the 312 transaxial
@@ -317,31 +317,34 @@ class ScatterSurrogate:
         net, meta = load_weights(path, geo.device)
         return cls(geo, net, meta["target_scale"], **kw)
 
-    def _forward(self, inp: torch.Tensor) -> torch.Tensor:
-        """The network's forward pass, replayed from a CUDA graph captured at the first call
-        (the ~30 launches of one inference cost more to issue than to run at batch 1)."""
-        if self._graph is None or self._graph_in.shape != inp.shape:
-            self._graph_in = inp.clone()
-            side = torch.cuda.Stream(inp.device)
-            side.wait_stream(torch.cuda.current_stream(inp.device))
+    def _predict_eager(self, emission: torch.Tensor, mu: torch.Tensor) -> torch.Tensor:
+        from .scatter_sinogram import crop_sino, network_input
+        inp, scale = network_input(self.geo, emission, mu)
+        out = self.net.forward(inp)                                     # (1, 56, 56, 320)
+        return crop_sino(out)[0] * (self.k * scale)
+
+    def predict(self, emission: torch.Tensor, mu: torch.Tensor) -> torch.Tensor:
+        """The network's sinogram for these volumes. The whole chain (input projections, the
+        U-Net, the output scaling: ~60 launches) is captured into a CUDA graph at the first call
+        and replayed, because at batch 1 issuing it costs more than running it."""
+        if self._graph is None or self._em_in.shape != emission.shape or self._mu_in.shape != mu.shape:
+            self._em_in, self._mu_in = emission.clone(), mu.clone()
+            dev = emission.device
+            side = torch.cuda.Stream(dev)
+            side.wait_stream(torch.cuda.current_stream(dev))
             with torch.cuda.stream(side):
-                self.net.forward(self._graph_in)  # allocates the activation buffers
-            torch.cuda.current_stream(inp.device).wait_stream(side)
+                self._predict_eager(self._em_in, self._mu_in)  # builds caches and activation buffers
+            torch.cuda.current_stream(dev).wait_stream(side)
             self._graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self._graph):
-                self._graph_out = self.net.forward(self._graph_in)
+                self._graph_out = self._predict_eager(self._em_in, self._mu_in)
             # the graph writes into these activation buffers: keep them alive even if the network
             # later reallocates its buffers for another batch shape
             self._graph_bufs = dict(self.net.buf)
-        self._graph_in.copy_(inp)
+        self._em_in.copy_(emission)
+        self._mu_in.copy_(mu)
         self._graph.replay()
-        return self._graph_out
-
-    def predict(self, emission: torch.Tensor, mu: torch.Tensor) -> torch.Tensor:
-        from .scatter_sinogram import crop_sino, network_input
-        inp, scale = network_input(self.geo, emission, mu)
-        out = self._forward(inp)                                        # (1, 56, 56, 320)
-        return crop_sino(out)[0] * (self.k * scale)
+        return self._graph_out.clone()
 
     def _spot_sss(self, emission: torch.Tensor, mu: torch.Tensor):
         """(bins, SSS of those bins) for ``spot_bins`` bins of the next pool; asynchronous."""
