@@ -368,9 +368,9 @@ class ScatterSurrogate:
         from .scatter_sinogram import sss_sinogram
         main = torch.cuda.current_stream(self.geo.device)
         self.side.wait_stream(main)
-        with torch.cuda.stream(self.side):
+        pred = self.predict(emission, mu)  # one graph launch: the GPU runs it while the host
+        with torch.cuda.stream(self.side):  # issues the spot check's kernels on the side stream
             bins, ref = self._spot_sss(emission, mu)
-        pred = self.predict(emission, mu)
         main.wait_stream(self.side)
         for t in (bins, ref):
             t.record_stream(main)
