@@ -71,6 +71,7 @@ class CoarseGeometry:
         self.bin_lors = torch.as_tensor(lors.astype(np.float32), device=self.device)
         self.ic = ImageConfig(list(VOL_SHAPE), [0.0, 0.0, 0.0], list(FOV_MM))
         self.scatter_points = self._scatter_points()
+        self.scatter_points_dev = torch.as_tensor(self.scatter_points, dtype=torch.float32, device=self.device)
 
     def _scatter_points(self) -> np.ndarray:
         """Every floor(50 mm / voxel) voxels, as preprocess.py:6-18 places them."""
@@ -167,7 +168,7 @@ def sss_pairs(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor, cpo
               pairs: torch.Tensor, low: int = 350, high: int = 650, resolution: float = 0.15) -> torch.Tensor:
     """SSS of crystal pairs given as int32 indices into the crystal positions ``cpos`` (m, 3):
     preprocessing of those m crystals, then srf_sss. No host synchronisation."""
-    sp = torch.as_tensor(geo.scatter_points, dtype=torch.float32, device=geo.device)
+    sp = geo.scatter_points_dev
     ic = geo.ic
     m, k = cpos.shape[0], sp.shape[0]
     Ld = torch.cat([cpos[:, None, :].expand(m, k, 3), sp[None, :, :].expand(m, k, 3)], 2).reshape(-1, 6)

@@ -288,6 +288,8 @@ class ScatterSurrogate:
         self.pools = self._make_pools(seed)
         self.calls = 0
         self._graph = self._graph_out = self._em_in = self._mu_in = None
+        self._spot_graphs = [None] * self.N_POOLS
+        self._pick = torch.zeros(spot_bins, dtype=torch.int64, device=geo.device)
 
     def _make_pools(self, seed: int):
         """Spot-check pools, built once: each is a random set of 48 of the 312 transaxial
@@ -327,7 +329,15 @@ class ScatterSurrogate:
         """The network's sinogram for these volumes. The whole chain (input projections, the
         U-Net, the output scaling: ~60 launches) is captured into a CUDA graph at the first call
         and replayed, because at batch 1 issuing it costs more than running it."""
+        self._ensure_graph(emission, mu)
+        self._em_in.copy_(emission)
+        self._mu_in.copy_(mu)
+        self._graph.replay()
+        return self._graph_out.clone()
+
+    def _ensure_graph(self, emission: torch.Tensor, mu: torch.Tensor) -> None:
         if self._graph is None or self._em_in.shape != emission.shape or self._mu_in.shape != mu.shape:
+            self._spot_graphs = [None] * self.N_POOLS  # they read the input buffers made here
             self._em_in, self._mu_in = emission.clone(), mu.clone()
             dev = emission.device
             side = torch.cuda.Stream(dev)
@@ -341,10 +351,6 @@ class ScatterSurrogate:
             # the graph writes into these activation buffers: keep them alive even if the network
             # later reallocates its buffers for another batch shape
             self._graph_bufs = dict(self.net.buf)
-        self._em_in.copy_(emission)
-        self._mu_in.copy_(mu)
-        self._graph.replay()
-        return self._graph_out.clone()
 
     def _spot_sss(self, emission: torch.Tensor, mu: torch.Tensor):
         """(bins, SSS of those bins) for ``spot_bins`` bins of the next pool; asynchronous."""
@@ -362,18 +368,52 @@ class ScatterSurrogate:
         bins, ref = self._spot_sss(emission, mu)
         return float(self._rel(pred.index_select(0, bins), ref).item())
 
+    def _spot_graph(self, j: int):
+        """Spot-check SSS of pool j on the bins self._pick selects, for the volumes in the
+        prediction graph's input buffers, captured into a CUDA graph at first use (its ~25
+        launches would otherwise be issued one by one). Returns (graph, bins, sss)."""
+        if self._spot_graphs[j] is None:
+            from .scatter_sinogram import sss_pairs
+            cand, local, cpos = self.pools[j]
+
+            def run():
+                return (cand.index_select(0, self._pick),
+                        sss_pairs(self.geo, self._em_in, self._mu_in, cpos, local.index_select(0, self._pick)))
+            self._pick.zero_()
+            side = torch.cuda.Stream(self.geo.device)
+            side.wait_stream(torch.cuda.current_stream(self.geo.device))
+            with torch.cuda.stream(side):
+                run()
+            torch.cuda.current_stream(self.geo.device).wait_stream(side)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                bins, ref = run()
+            self._spot_graphs[j] = (g, bins, ref)
+        return self._spot_graphs[j]
+
     def estimate(self, emission: torch.Tensor, mu: torch.Tensor, fallback: bool = True):
         """(sinogram, record). With ``fallback=False`` the prediction is returned even when its
-        spot check failed (the record still says so)."""
+        spot check failed (the record still says so). The prediction and the spot-check SSS are
+        two graph launches on two streams, so they run side by side."""
         from .scatter_sinogram import sss_sinogram
-        main = torch.cuda.current_stream(self.geo.device)
-        self.side.wait_stream(main)
-        pred = self.predict(emission, mu)  # one graph launch: the GPU runs it while the host
-        with torch.cuda.stream(self.side):  # issues the spot check's kernels on the side stream
-            bins, ref = self._spot_sss(emission, mu)
+        dev = self.geo.device
+        main = torch.cuda.current_stream(dev)
+        self._ensure_graph(emission, mu)
+        j = self.calls % self.N_POOLS
+        self.calls += 1
+        g, bins, ref = self._spot_graph(j)
+        self._em_in.copy_(emission)
+        self._mu_in.copy_(mu)
+        ready = torch.cuda.Event()
+        ready.record(main)
+        self._graph.replay()
+        pred = self._graph_out.clone()
+        with torch.cuda.stream(self.side):
+            self.side.wait_event(ready)
+            n_c = self.pools[j][0].numel()
+            self._pick.copy_(torch.randint(0, n_c, (self.spot_bins,), generator=self.gen, device=dev))
+            g.replay()
         main.wait_stream(self.side)
-        for t in (bins, ref):
-            t.record_stream(main)
         err = float(self._rel(pred.index_select(0, bins), ref).item())
         if not (err <= self.fallback_tol):
             if fallback:
