@@ -277,18 +277,20 @@ __device__ __forceinline__ void slab_voxels(const LorRun &r, int ip, bool keep, 
     const int cq1 = ifloor(qq1), cq2 = ifloor(qq2);
     const int cz1 = ifloor(zz1), cz2 = ifloor(zz2);
     const bool dq = cq1 != cq2, dz = cz1 != cz2;
-    const bool R = keep && cq1 >= (dq ? -1 : 0) && cq1 < r.nq && cz1 >= (dz ? -1 : 0) && cz1 < r.nz;
     const float fq = ((float)cq2 - qq1) * r.invq;  // used only when dq
     const float fz = ((float)cz2 - zz1) * r.invz;  // used only when dz
     const float f0 = fminf(dq ? fq : 1.0f, dz ? fz : 1.0f);
     const float f2 = 1.0f - fmaxf(dq ? fq : 0.0f, dz ? fz : 0.0f);
     const int32_t base = ip * r.sp;
     const int32_t q1o = cq1 * r.sq, q2o = cq2 * r.sq, z1o = cz1 * r.szs, z2o = cz2 * r.szs;
-    const bool v0 = R && (cq1 | cz1) >= 0;
-    const bool far_in = cq2 < r.nq && cz2 < r.nz;
-    const bool v2 = R && (dq || dz) && far_in;
+    // the reference's range tests, with cq1 <= cq2 and cz1 <= cz2: c in [0, n) as one unsigned compare
+    const bool a = (unsigned)cq1 < (unsigned)r.nq, b = (unsigned)cz1 < (unsigned)r.nz;
+    const bool c = (unsigned)cq2 < (unsigned)r.nq, d = (unsigned)cz2 < (unsigned)r.nz;
+    const bool q1m = cq1 >= -1, z1m = cz1 >= -1;
+    const bool v0 = keep && a && b;
+    const bool v2 = keep && (dq || dz) && c && d && q1m && z1m;
     const bool qfirst = fq > fz;
-    const bool v1 = R && dq && dz && (qfirst ? (cq1 >= 0 && cz2 < r.nz) : (cq2 < r.nq && cz1 >= 0));
+    const bool v1 = keep && dq && dz && (qfirst ? (a && d && z1m) : (c && b && q1m));
     o[0] = v0 ? base + q1o + z1o : 0;
     w[0] = v0 ? f0 * wt : 0.0f;
     o[2] = v2 ? base + q2o + z2o : 0;
@@ -313,7 +315,7 @@ __device__ __forceinline__ void candidates_fast(const LorRun &r, const GridK &k,
             bad = fabsf(e2 - k.e2cut) <= k.e2tol;
             keep = keep && (e2 >= k.e2cut);
         }
-        w_tof = exp2f(e2);  // exp(-t2 / 2); the amplitude is in wc
+        asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(w_tof) : "f"(e2));  // exp(-t2 / 2), amplitude in wc
     }
     const float pp1 = __fsub_rn((float)ip, r.np2);
     const float pp2 = __fadd_rn(pp1, 1.0f);
