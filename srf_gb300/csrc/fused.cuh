@@ -372,6 +372,8 @@ int fused_projection(const float *lors, int64_t n, int stride, const float *tof,
 int fused_backprojection(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
                          const Grid &g, const TofParams &tp, const float *values, const View &v,
                          const View &vt, cudaStream_t s);
+// Block-full sensitivity image: backprojection of 1 along every ordered pair of table rows.
+int fused_emap(const float *table, int nb, int m, const Grid &g, const View &v, const View &vt, cudaStream_t s);
 // The projector and its exact adjoint for nb <= 8 images at element offsets b * bstride.
 int fused_projection_batch(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
                            const Grid &g, const TofParams &tp, int nb, int64_t bstride, const View &v,

@@ -285,6 +285,94 @@ int fused_backprojection(const float *lors, int64_t n, int stride, const float *
                : launch_trace_fused<false, MODE_BACK>(lors, n, stride, nullptr, 1, g, tp, values, nullptr, v, vt, s);
 }
 
+// ---------------------------------------------------------------- sensitivity image
+// Backprojection of 1 along every ordered crystal pair of the block-full sensitivity image, on the
+// fused traversal: LOR k = ((i*nb + j)*m + a)*m + b runs from table row i*m + a to row j*m + b
+// (the table holds the reference's float32 crystal positions), generated on the fly.
+__device__ __forceinline__ void emap_endpoints(const float *__restrict__ table, int nb, int m, int64_t k,
+                                               float (&lv)[6]) {
+    const int64_t mm = (int64_t)m * m;
+    const int64_t blk = k / mm, rem = k - blk * mm;
+    const int i = (int)(blk / nb), j = (int)(blk - (blk / nb) * nb);
+    const int a = (int)(rem / m), b = (int)(rem - (rem / m) * m);
+    const float *e1 = table + 3 * ((int64_t)i * m + a);
+    const float *e2 = table + 3 * ((int64_t)j * m + b);
+    lv[0] = __ldg(e1); lv[1] = __ldg(e1 + 1); lv[2] = __ldg(e1 + 2);
+    lv[3] = __ldg(e2); lv[4] = __ldg(e2 + 1); lv[5] = __ldg(e2 + 2);
+}
+
+template <int G, int U>
+__device__ __forceinline__ void emap_warp(LorRec *wrecs, const float *__restrict__ table, int nb, int m, int64_t n,
+                                          const Grid &g, const GridK &k, const TofParams &tp, const View &v,
+                                          const View &vt, int64_t base) {
+    constexpr int GPW = 32 / G;
+    const int lane32 = threadIdx.x & 31;
+    const int lane = threadIdx.x & (G - 1);
+    const int gi = lane32 / G;
+    const bool have_t = vt.ptr != nullptr;
+    {
+        const int64_t i = base + lane32;
+        LorRec R = {};
+        R.lo = 1;
+        if (i < n) {
+            float lv[6];
+            emap_endpoints(table, nb, m, i, lv);
+            R = setup_rec<false>(lv, 0.0f, 1.0f, g, k);
+        }
+        store_rec(&wrecs[lane32], R);
+    }
+    __syncwarp();
+    for (int j0 = 0; j0 < 32; j0 += GPW) {
+        const int j = j0 + gi;
+        const LorRec R = load_rec(&wrecs[j]);
+        const int64_t i = base + j;
+        if (R.flags & F_TIE) {  // the backprojector's own axis differs from the projector's: generic path
+            float lv[6];
+            emap_endpoints(table, nb, m, i, lv);
+            tie_backproject<G, false>(lv, 0.0f, 1.0f, lane, g, tp, v, vt);
+            continue;
+        }
+        if (!(R.flags & F_VALID)) continue;
+        const LorRun run = make_run(R, g, k, v.st, vt.st, have_t);
+        float *im = (!run.xdom && have_t) ? vt.ptr : v.ptr;
+        int32_t o[U][3];
+        float w[U][3];
+        bool pm[U];
+        for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
+            chunk_candidates<false, U>(run, k, c0, lane, G, o, w, pm);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    if (w[u][c] != 0.0f) atomicAdd(im + o[u][c], w[u][c]);
+        }
+    }
+    __syncwarp();
+}
+
+template <int G, int U, int MINB>
+__global__ void __launch_bounds__(kOsemBlock, MINB)
+k_emap_fused(const float *__restrict__ table, int nb, int m, Grid g, View v, View vt) {
+    __shared__ LorRec recs[kOsemBlock / 32][32];
+    const int wib = threadIdx.x >> 5;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const TofParams tp{0, 0, 0};
+    const GridK k = make_gridk<false>(g, tp);
+    const int64_t n = (int64_t)nb * nb * (int64_t)m * m;
+    for (int64_t base = warp * 32; base < n; base += nwarps * 32)
+        emap_warp<G, U>(recs[wib], table, nb, m, n, g, k, tp, v, vt, base);
+}
+
+int fused_emap(const float *table, int nb, int m, const Grid &g, const View &v, const View &vt, cudaStream_t s) {
+    const int64_t n = (int64_t)nb * nb * (int64_t)m * m;
+    if (n == 0) return ok();
+    auto kern = k_emap_fused<32, 4, 5>;
+    unsigned blocks = grid_for(kern, n, kOsemBlock, 0, kOsemBlock);
+    kern<<<blocks, kOsemBlock, 0, s>>>(table, nb, m, g, v, vt);
+    return check_cuda("emap kernel launch");
+}
+
 // ---------------------------------------------------------------- batched projector / adjoint
 // The projector (MODE_PROJ) and its exact adjoint (MODE_ADJ: projector rules, projector weights
 // with 1/L^2, scattered) for nb <= kMaxBatch images that share the grid and the LORs: image b at
