@@ -338,6 +338,20 @@ int srf_cnn_rel_mse(const float *pred, const float *target, const float *mask, c
 int srf_cnn_adam(float *w, float *m, float *v, const float *g, void *bf16_copy, int64_t n, float lr,
                  float b1, float b2, float eps, int32_t step, void *stream);
 
+/* ------------------------------------------------------------------ surrogate spot check */
+/* No counterpart in the reference: the spot-check correction of the network's scatter sinogram.
+ * pred: the estimate over nbins bins; bins[0..n), ref[0..n): the spot-check samples (bin, SSS
+ * value); phi: k <= 12 basis rows of nbins values each (row j at phi + j * nbins).
+ * beta minimises, over the even samples s, sum (ref[s] - pred[b] * sum_j beta_j phi_j[b])^2 with
+ * b = bins[s], plus ridge * (trace / k) * |beta|^2 of the normal matrix (FP64 normal equations,
+ * Cholesky); beta = e0 when that matrix is zero or not positive definite. Samples whose bin lies
+ * outside [0, nbins) are left out. out (k + 2 floats): beta, then the relative L2 difference of
+ * the corrected prediction from ref over the odd samples, then the same for the uncorrected one. */
+int srf_spot_fit(const float *pred, int64_t nbins, const int64_t *bins, const float *ref, int32_t n,
+                 const float *phi, int32_t k, double ridge, float *out, void *stream);
+/* x[i] *= sum_j beta[j] * phi[j * n + i], beta (k <= 12 values) and phi on the device. */
+int srf_scale_by_basis(float *x, int64_t n, const float *phi, int32_t k, const float *beta, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,3 +101,31 @@ def head8_grads(x, w, gout):
     gw = np.einsum("ndhwq,ndhwc->qc", gq, x)
     gb = gq.sum(axis=(0, 1, 2, 3))
     return gx, gw, gb
+
+
+def spot_fit(pred, bins, ref, phi, ridge=1e-6):
+    """The surrogate's spot-check correction (srf_spot_fit): beta minimising, over the even
+    samples s, (ref[s] - pred[b] * beta . phi[:, b])^2 with b = bins[s], plus ridge * (trace / k)
+    * |beta|^2 of the normal matrix; e0 when that matrix is zero. Samples with a bin outside
+    [0, len(pred)) are left out. Returns (beta, judged, uncorrected): the relative L2 differences
+    of the corrected and uncorrected prediction from ref over the odd samples."""
+    pred = np.asarray(pred, np.float64)
+    phi = np.asarray(phi, np.float64)
+    bins = np.asarray(bins, np.int64)
+    ref = np.asarray(ref, np.float64)
+    k, nb = phi.shape
+    keep = (bins >= 0) & (bins < nb)
+    even = np.zeros(bins.size, bool)
+    even[0::2] = True
+    fi, ju = np.flatnonzero(even & keep), np.flatnonzero(~even & keep)
+    a = pred[bins[fi]][None, :] * phi[:, bins[fi]]
+    ata = a @ a.T
+    tr = float(np.trace(ata))
+    if tr > 0.0 and np.isfinite(tr):
+        beta = np.linalg.solve(ata + (ridge * tr / k) * np.eye(k), a @ ref[fi])
+    else:
+        beta = np.eye(k)[0]
+    p, y = pred[bins[ju]], ref[ju]
+    den = max(float(np.linalg.norm(y)), 1e-30)
+    judged = float(np.linalg.norm(p * (beta @ phi[:, bins[ju]]) - y)) / den
+    return beta, judged, float(np.linalg.norm(p - y)) / den

@@ -30,7 +30,7 @@ EXPORTS = (
     "srf_backprojection_tof_noalloc", "srf_listmode_snap", "srf_lm2sino", "srf_attenuation",
     "srf_conv3d_fwd", "srf_conv3d_wgrad", "srf_conv3d_flip_weights", "srf_cnn_relu_bwd",
     "srf_cnn_bias_grad", "srf_cnn_pool2", "srf_cnn_upsample2", "srf_cnn_add", "srf_cnn_head8", "srf_calib_l2", "srf_calib_sink_size",
-    "srf_cnn_rel_mse", "srf_cnn_adam",
+    "srf_cnn_rel_mse", "srf_cnn_adam", "srf_spot_fit", "srf_scale_by_basis",
 )
 
 
@@ -101,6 +101,10 @@ def f32x3(v: Sequence[float]):
 
 def f32(v: float):
     return ctypes.c_float(float(v))
+
+
+def f64(v: float):
+    return ctypes.c_double(float(v))
 
 
 def i32(v: int):

@@ -18,8 +18,9 @@ channel slices the decoder reads. The network runs on the 2x-pooled sinogram and
 the full-resolution sinogram directly (no interpolation floor).
 
 ``ScatterSurrogate`` wraps the network with SSS as the judge: ``estimate`` predicts the scatter
-sinogram and, when a spot-check SSS on a subset of bins differs by more than ``fallback_tol``
-relative L2, returns the full SSS instead.
+sinogram, runs SSS on a random subset of bins, fits a smooth multiplicative correction of the
+prediction on half of those bins and judges the corrected prediction on the other half; when the
+judged relative L2 difference exceeds ``fallback_tol`` it returns the full SSS instead.
 """
 from __future__ import annotations
 
@@ -30,7 +31,7 @@ from typing import Dict, List, Optional, Tuple
 import numpy as np
 import torch
 
-from ._lib import call, f32, i32, i64, ptr, stream_ptr
+from ._lib import call, f32, f64, i32, i64, ptr, stream_ptr
 
 BF16 = torch.bfloat16
 F32 = torch.float32
@@ -267,14 +268,57 @@ DEFAULT_WEIGHTS = __file__.rsplit("/", 1)[0] + "/weights/scatter_unet.npz"
 
 
 # ---------------------------------------------------------------- surrogate with SSS as the judge
+def correction_basis(device) -> torch.Tensor:
+    """(9, 51 * 52 * 312) FP32 smooth functions of a bin's position in the coarse sinogram, the
+    basis of the spot-check correction: 1, the radial offset and the plane (each to second order,
+    normalised to [-1, 1]), and the first and second harmonics of the LOR's mid-point angle
+    psi = 2 pi (view + 39 + 1.5 radial) / 312, the crystals of a bin sitting at views v and
+    v + 78 + 3 radial (bins are (plane, radial, view), view fastest)."""
+    from .scatter_sinogram import PLANES, RADIAL, RADIAL_OFF, RADIAL_STEP, VIEWS
+    P, R, V = PLANES - 1, RADIAL, VIEWS
+    shape = (P, R, V)
+    p = torch.arange(P, dtype=torch.float64, device=device).view(P, 1, 1).expand(shape).reshape(-1)
+    r = torch.arange(R, dtype=torch.float64, device=device).view(1, R, 1).expand(shape).reshape(-1)
+    v = torch.arange(V, dtype=torch.float64, device=device).view(1, 1, V).expand(shape).reshape(-1)
+    pn = (p - 0.5 * (P - 1)) / (0.5 * (P - 1))
+    rn = (r - 0.5 * (R - 1)) / (0.5 * (R - 1))
+    psi = (2.0 * math.pi / V) * (v + 0.5 * (V // 2 - RADIAL_OFF) + 0.5 * RADIAL_STEP * r)
+    rows = [torch.ones_like(p), rn, rn * rn, pn, pn * pn, torch.cos(psi), torch.sin(psi),
+            torch.cos(2 * psi), torch.sin(2 * psi)]
+    return torch.stack(rows, 0).to(F32).contiguous()
+
+
+def spot_fit(pred: torch.Tensor, bins: torch.Tensor, ref: torch.Tensor, basis: torch.Tensor,
+             out: torch.Tensor, ridge: float = 1e-6) -> None:
+    """srf_spot_fit: out[:k] = coefficients of the correction pred * (beta . basis) fitted to the
+    even spot samples (bins, ref), out[k] / out[k + 1] = relative L2 difference of the corrected /
+    uncorrected prediction on the odd samples. Asynchronous on the current stream."""
+    k, nb = basis.shape
+    assert pred.dtype == F32 and ref.dtype == F32 and basis.dtype == F32 and bins.dtype == torch.int64
+    assert pred.numel() == nb and out.numel() >= k + 2 and bins.numel() == ref.numel()
+    call("srf_spot_fit", ptr(pred), i64(nb), ptr(bins), ptr(ref), i32(bins.numel()), ptr(basis), i32(k),
+         f64(ridge), ptr(out), stream_ptr(pred.device))
+
+
+def scale_by_basis(x: torch.Tensor, basis: torch.Tensor, beta: torch.Tensor) -> None:
+    """srf_scale_by_basis: x *= beta . basis, in place (beta on the device)."""
+    k, nb = basis.shape
+    assert x.dtype == F32 and x.numel() == nb and beta.numel() >= k
+    call("srf_scale_by_basis", ptr(x), i64(nb), ptr(basis), i32(k), ptr(beta), stream_ptr(x.device))
+
+
 class ScatterSurrogate:
     """Coarse-sinogram scatter estimate from the network, checked against SSS on a few bins.
 
     ``estimate(emission, mu)`` returns the flat (51 * 52 * 312) scatter sinogram in SSS units and
-    a record of what happened: the relative L2 difference between the prediction and a fresh SSS
-    on ``spot_bins`` random bins, and whether that exceeded ``fallback_tol`` so that the full SSS
-    was returned instead. The spot-check SSS runs on a side stream while the network runs on the
-    caller's stream; the only host synchronisation is the final comparison."""
+    a record of what happened. A fresh SSS on ``spot_bins`` random bins serves twice: on the even
+    samples it fits a smooth multiplicative correction (``correction_basis``: global scale,
+    radial and plane trends, first and second view harmonics), and on the odd samples, which the
+    fit has not seen, it judges the corrected prediction. The record holds that judged relative
+    L2 difference, the uncorrected one, the coefficients, and whether the judged difference
+    exceeded ``fallback_tol`` so that the full SSS was returned instead. The spot-check SSS runs
+    on a side stream while the network runs on the caller's stream; the only host
+    synchronisation is one read of the spot samples."""
 
     N_POOLS = 8
     POOL_POSITIONS = 48
@@ -290,6 +334,10 @@ class ScatterSurrogate:
         self._graph = self._graph_out = self._em_in = self._mu_in = None
         self._spot_graphs = [None] * self.N_POOLS
         self._pick = torch.zeros(spot_bins, dtype=torch.int64, device=geo.device)
+        self.basis = correction_basis(geo.device)
+        k = self.basis.shape[0]
+        self._fit = torch.zeros(k + 2, dtype=F32, device=geo.device)      # beta, judged, uncorrected
+        self._fit_host = torch.zeros(k + 2, dtype=F32).pin_memory()
 
     def _make_pools(self, seed: int):
         """Spot-check pools, built once: each is a random set of 48 of the 312 transaxial
@@ -392,9 +440,9 @@ class ScatterSurrogate:
         return self._spot_graphs[j]
 
     def estimate(self, emission: torch.Tensor, mu: torch.Tensor, fallback: bool = True):
-        """(sinogram, record). With ``fallback=False`` the prediction is returned even when its
-        spot check failed (the record still says so). The prediction and the spot-check SSS are
-        two graph launches on two streams, so they run side by side."""
+        """(sinogram, record). With ``fallback=False`` the corrected prediction is returned even
+        when its spot check failed (the record still says so). The prediction and the spot-check
+        SSS are two graph launches on two streams, so they run side by side."""
         from .scatter_sinogram import sss_sinogram
         dev = self.geo.device
         main = torch.cuda.current_stream(dev)
@@ -414,12 +462,24 @@ class ScatterSurrogate:
             self._pick.copy_(torch.randint(0, n_c, (self.spot_bins,), generator=self.gen, device=dev))
             g.replay()
         main.wait_stream(self.side)
-        err = float(self._rel(pred.index_select(0, bins), ref).item())
+        # fit and judge the correction, apply it (discarded if the judge fails), read k + 2 numbers
+        k = self.basis.shape[0]
+        spot_fit(pred, bins, ref, self.basis, self._fit)
+        scale_by_basis(pred, self.basis, self._fit)
+        self._fit_host.copy_(self._fit, non_blocking=True)
+        done = torch.cuda.Event()
+        done.record(main)
+        done.synchronize()
+        h = self._fit_host.tolist()
+        err = h[k]
+        info = {"spot_rel_l2": err, "spot_rel_l2_uncorrected": h[k + 1], "correction": h[:k],
+                "fallback": False}
         if not (err <= self.fallback_tol):
             if fallback:
-                return sss_sinogram(self.geo, emission, mu), {"spot_rel_l2": err, "fallback": True}
-            return pred, {"spot_rel_l2": err, "fallback": False, "spot_failed": True}
-        return pred, {"spot_rel_l2": err, "fallback": False}
+                info["fallback"] = True
+                return sss_sinogram(self.geo, emission, mu), info
+            info["spot_failed"] = True
+        return pred, info
 
 
 # ---------------------------------------------------------------- training

@@ -174,3 +174,41 @@ def test_unet_gradient_matches_finite_differences_and_trains(cuda_lib):
         net.backward(grad)
         net.step(3e-3)
     assert loss_only() < 0.5 * l0
+
+
+def test_spot_fit_and_scale_by_basis_match_the_oracle(cuda_lib, cnn):
+    """The surrogate's spot-check correction kernels against the oracle: srf_spot_fit (FP64
+    normal equations and Cholesky in one block) on a noisy prediction with a planted smooth
+    correction, with repeated and out-of-range sample bins; srf_scale_by_basis applying it; and a
+    prediction that is zero everywhere, which gets the identity correction."""
+    from srf_gb300.surrogate import correction_basis, scale_by_basis, spot_fit
+    dev = torch.device("cuda", 0)
+    basis = correction_basis(dev)
+    phi = basis.double().cpu().numpy()
+    k, nb = phi.shape
+    rng = np.random.default_rng(11)
+    ref_full = rng.uniform(0.5, 2.0, nb)
+    beta_true = np.array([0.9, -0.04, 0.03, 0.02, -0.05, 0.01, 0.02, -0.03, 0.01])
+    pred = (ref_full / (beta_true @ phi) * (1.0 + 0.05 * rng.standard_normal(nb))).astype(np.float32)
+    bins = rng.integers(0, nb, 2048)
+    bins[7] = bins[9]
+    bins[5], bins[8] = nb + 3, -1                  # left out by the kernel and the oracle
+    ref = ref_full[np.clip(bins, 0, nb - 1)].astype(np.float32)
+    pred_d = torch.as_tensor(pred, device=dev)
+    bins_d = torch.as_tensor(bins, device=dev)
+    ref_d = torch.as_tensor(ref, device=dev)
+    out = torch.zeros(k + 2, device=dev)
+    spot_fit(pred_d, bins_d, ref_d, basis, out)
+    beta, judged, raw = cnn.spot_fit(pred, bins, ref, phi)
+    got = out.cpu().numpy().astype(np.float64)
+    assert np.allclose(got[:k], beta, rtol=1e-5, atol=1e-6)
+    assert np.allclose(beta, beta_true, atol=0.01)
+    assert abs(got[k] - judged) <= 1e-5 * judged and abs(got[k + 1] - raw) <= 1e-5 * raw
+    assert 0.03 < judged < 0.07 < raw
+    x = pred_d.clone()
+    scale_by_basis(x, basis, out)
+    want = pred.astype(np.float64) * (got[:k] @ phi)
+    assert rel_l2(x.cpu().numpy(), want) <= 1e-6
+    spot_fit(torch.zeros_like(pred_d), bins_d, ref_d, basis, out)
+    got = out.cpu().numpy()
+    assert np.array_equal(got[:k], np.eye(k)[0]) and abs(got[k] - 1.0) < 1e-6 and abs(got[k + 1] - 1.0) < 1e-6

@@ -2,8 +2,9 @@
 single-scatter simulation, on phantoms that were not in its training set (training used seeds
 0..1999, these start at 1,000,000).
 
-* the network's sinogram is within ~7 % relative L2 of SSS on average, and the guarded estimate
-  is either a prediction that passed its spot check (5 %) or SSS itself;
+* the network's sinogram is within ~7 % relative L2 of SSS on average, the correction fitted on
+  half of the spot-check bins brings it closer, and the guarded estimate is either a corrected
+  prediction that passed its spot check on the other half (5 %) or SSS itself;
 * a network that is wrong is caught by the spot check and SSS is returned instead;
 * TOF OSEM with the network's scatter matches OSEM with SSS scatter within 1 % relative L2,
   while the image without scatter correction is far off, and the network path (with its spot
@@ -40,25 +41,27 @@ def test_guarded_estimate_stays_within_tolerance_of_sss(geo, sur):
     a caller gets is either the network's, when its spot check passed (then it is close to SSS on
     the whole sinogram too), or SSS itself."""
     from srf_gb300.scatter_sinogram import random_phantom, sss_sinogram
-    errs = []
-    for sd in range(1_000_100, 1_000_106):
+    errs, corrected = [], []
+    for sd in range(1_000_100, 1_000_108):
         em, mu = random_phantom(sd, device=geo.device)
         ref = sss_sinogram(geo, em, mu)
         errs.append(rel(sur.predict(em, mu), ref))
+        corrected.append(rel(sur.estimate(em, mu, fallback=False)[0], ref))
         est, info = sur.estimate(em, mu)
         if info["fallback"]:
             assert info["spot_rel_l2"] > 0.05 and rel(est, ref) <= 1e-6
         else:
             assert info["spot_rel_l2"] <= 0.05 and rel(est, ref) <= 0.075
     assert sum(errs) / len(errs) <= 0.09
+    assert sum(corrected) < sum(errs)
 
 
 def test_wrong_network_falls_back_to_sss(geo):
+    """An untrained network: no smooth correction makes its output a scatter sinogram."""
     from srf_gb300.scatter_sinogram import random_phantom, sss_sinogram
-    from srf_gb300.surrogate import DEFAULT_WEIGHTS, ScatterSurrogate, load_weights
-    net, meta = load_weights(DEFAULT_WEIGHTS, geo.device)
-    net.hb += 3.0  # shifts every prediction far from the SSS sinogram
-    bad = ScatterSurrogate(geo, net, meta["target_scale"])
+    from srf_gb300.surrogate import DEFAULT_WEIGHTS, ScatterSurrogate, UNet3D, load_weights
+    _, meta = load_weights(DEFAULT_WEIGHTS, geo.device)
+    bad = ScatterSurrogate(geo, UNet3D(seed=7, device=geo.device), meta["target_scale"])
     em, mu = random_phantom(1_000_103, device=geo.device)
     est, info = bad.estimate(em, mu)
     assert info["fallback"] and info["spot_rel_l2"] > 0.05

@@ -172,3 +172,34 @@ def test_surrogate_spot_pools_index_their_own_crystals():
         pr = geo.pairs[cand.numpy()]
         for col in range(2):
             assert np.array_equal(geo.vpos[pr[:, col]], cpos.numpy()[local[:, col].numpy()])
+
+
+def test_surrogate_correction_basis_and_fit():
+    """The spot-check correction: its basis is 1, radial and plane trends in [-1, 1] and the
+    harmonics of each bin's LOR mid-point angle; the oracle's fit recovers a correction planted
+    in that basis from the even samples of 2,048 sampled bins and judges it exact on the odd
+    ones, and a prediction that is zero on every sample gets none."""
+    import math
+    import torch
+    from cnn_oracle import spot_fit
+    from srf_gb300.scatter_sinogram import PLANES, RADIAL, VIEWS
+    from srf_gb300.surrogate import correction_basis
+    phi = correction_basis(torch.device("cpu")).double().numpy()
+    assert phi.shape == (9, (PLANES - 1) * RADIAL * VIEWS)
+    flat = lambda p, r, v: (p * RADIAL + r) * VIEWS + v
+    j = flat(PLANES - 2, RADIAL - 1, VIEWS - 1)
+    psi = 2 * math.pi * (VIEWS - 1 + 39 + 1.5 * (RADIAL - 1)) / VIEWS
+    want = [1, 1, 1, 1, 1, math.cos(psi), math.sin(psi), math.cos(2 * psi), math.sin(2 * psi)]
+    assert np.allclose(phi[:, j], want, atol=1e-6)
+    assert np.allclose(phi[:5, flat(0, 0, 0)], [1, -1, 1, -1, 1])
+    rng = np.random.default_rng(3)
+    ref = rng.uniform(0.5, 2.0, phi.shape[1])
+    beta_true = np.array([1.2, 0.05, -0.04, 0.03, 0.02, 0.01, -0.02, 0.03, 0.01])
+    pred = ref / (beta_true @ phi)
+    bins = rng.choice(phi.shape[1], 2048, replace=False)
+    beta, judged, raw = spot_fit(pred, bins, ref[bins], phi)
+    assert np.allclose(beta, beta_true, rtol=1e-4, atol=1e-5)
+    assert np.allclose(pred * (beta @ phi), ref, rtol=1e-4)
+    assert judged < 1e-5 and raw > 0.05
+    e0, _, _ = spot_fit(np.zeros(phi.shape[1]), bins[:16], rng.uniform(size=16), phi)
+    assert np.array_equal(e0, np.eye(9)[0])
