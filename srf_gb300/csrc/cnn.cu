@@ -58,67 +58,135 @@ __device__ __forceinline__ void warp_mma_step(const __nv_bfloat16 (*As)[kCPad],
     }
 }
 
-// y[v, co] = act(b[co] + sum_{tap, ci} x[v + tap - 1, ci] w[co, tap, ci])
+// One k-step of a warp on a BM x BN tile: MT 16-row m-tiles from row r0 of As, NT 8-column
+// n-tiles of Bs (stored [n][k]).
+template <int MT, int NT>
+__device__ __forceinline__ void warp_mma_tile(const __nv_bfloat16 (*As)[kCPad], const __nv_bfloat16 (*Bs)[kCPad],
+                                              int r0, float (&acc)[MT][NT][4]) {
+    const int lane = threadIdx.x & 31, grp = lane >> 2, tig = lane & 3;
+    uint32_t a[MT][4];
+#pragma unroll
+    for (int m = 0; m < MT; ++m) {
+        const int r = r0 + m * 16 + grp;
+        a[m][0] = lds32(&As[r][tig * 2]);
+        a[m][1] = lds32(&As[r + 8][tig * 2]);
+        a[m][2] = lds32(&As[r][tig * 2 + 8]);
+        a[m][3] = lds32(&As[r + 8][tig * 2 + 8]);
+    }
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+        uint32_t b[2];
+        b[0] = lds32(&Bs[j * 8 + grp][tig * 2]);
+        b[1] = lds32(&Bs[j * 8 + grp][tig * 2 + 8]);
+#pragma unroll
+        for (int m = 0; m < MT; ++m) mma_bf16(acc[m][j], a[m], b);
+    }
+}
+
+// y[v, co] = act(b[co] + sum_{tap, ci} x[v + tap - 1, ci] w[co, tap, ci]) on BM-voxel x
+// BN-channel tiles (4 warps, each BM/4 rows x BN columns). K runs over (tap, 16-channel chunk)
+// steps; the next step's gathered rows and weight slice are loaded into registers while the
+// tensor cores work on the current one and are stored into the other of two shared-memory
+// buffers, so each step costs one barrier and no exposed global latency.
+template <int BM, int BN>
 __global__ void __launch_bounds__(128)
 k_conv3d_fwd(const __nv_bfloat16 *__restrict__ x, Act xa, int cin, const __nv_bfloat16 *__restrict__ wt,
              const float *__restrict__ bias, int cout, int relu, __nv_bfloat16 *__restrict__ y, Act ya,
              float *__restrict__ yf) {
-    __shared__ __align__(16) __nv_bfloat16 As[kCM][kCPad];
-    __shared__ __align__(16) __nv_bfloat16 Bs[kCN][kCPad];
+    constexpr int MT = BM / 64, NT = BN / 8;  // m-tiles per warp, n-tiles
+    constexpr int AS = BM / 64;               // A slots (half rows of 8 channels) per thread
+    static_assert(2 * BN <= 128, "one B slot per thread");
+    __shared__ __align__(16) __nv_bfloat16 As[2][BM][kCPad];
+    __shared__ __align__(16) __nv_bfloat16 Bs[2][BN][kCPad];
     const int64_t nvox = (int64_t)xa.d * xa.h * xa.w;
-    const int64_t v0 = (int64_t)blockIdx.x * kCM;
-    const int co0 = blockIdx.y * kCN;
+    const int64_t v0 = (int64_t)blockIdx.x * BM;
+    const int co0 = blockIdx.y * BN;
     const int nb = blockIdx.z;
     const int tid = threadIdx.x, warp = tid >> 5;
-    float acc[8][4] = {};
-    // loader role: thread t loads half a row (8 channels) of A and of B
-    const int lr = tid >> 1, lh = (tid & 1) * 8;
-    const int64_t lv = v0 + lr;
-    const bool lv_ok = lv < nvox;
-    const int lz = lv_ok ? (int)(lv / ((int64_t)xa.h * xa.w)) : 0;
-    const int lrem = lv_ok ? (int)(lv - (int64_t)lz * xa.h * xa.w) : 0;
-    const int ly = lrem / xa.w, lx = lrem - ly * xa.w;
     const __nv_bfloat16 *xb = x + (int64_t)nb * nvox * xa.cstride + xa.coff;
-    const int lco = co0 + lr;
-    for (int tap = 0; tap < 27; ++tap) {
-        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-        const int zz = lz + dz, yy = ly + dy, xx = lx + dx;
-        const bool in = lv_ok && zz >= 0 && zz < xa.d && yy >= 0 && yy < xa.h && xx >= 0 && xx < xa.w;
-        const int64_t src = in ? (((int64_t)zz * xa.h + yy) * xa.w + xx) * xa.cstride : 0;
-        for (int c0 = 0; c0 < cin; c0 += kCK) {
-            uint4 av = make_uint4(0, 0, 0, 0), bv = make_uint4(0, 0, 0, 0);
-            if (in) av = *reinterpret_cast<const uint4 *>(xb + src + c0 + lh);
-            if (lco < cout) bv = *reinterpret_cast<const uint4 *>(wt + ((int64_t)lco * 27 + tap) * cin + c0 + lh);
-            *reinterpret_cast<uint4 *>(&As[lr][lh]) = av;
-            *reinterpret_cast<uint4 *>(&Bs[lr][lh]) = bv;
-            __syncthreads();
-            warp_mma_step(As, Bs, warp * 16, acc);
-            __syncthreads();
-        }
+    // A slots: row tid / 2 + 64 i, channel half (tid & 1) * 8
+    const int lh = (tid & 1) * 8;
+    int lr[AS], lz[AS], ly[AS], lx[AS];
+    bool lok[AS];
+#pragma unroll
+    for (int i = 0; i < AS; ++i) {
+        lr[i] = (tid >> 1) + 64 * i;
+        const int64_t v = v0 + lr[i];
+        lok[i] = v < nvox;
+        const int z = lok[i] ? (int)(v / ((int64_t)xa.h * xa.w)) : 0;
+        const int rem = lok[i] ? (int)(v - (int64_t)z * xa.h * xa.w) : 0;
+        lz[i] = z;
+        ly[i] = rem / xa.w;
+        lx[i] = rem - ly[i] * xa.w;
     }
-    // epilogue: rows (warp*16 + grp, +8), columns (j*8 + tig*2, +1)
+    // B slot: threads [0, 2 BN) load output channel co0 + tid / 2
+    const bool bload = tid < 2 * BN;
+    const int br = tid >> 1, bco = co0 + br;
+    const bool bok = bload && bco < cout;
+    uint4 ra[AS], rb = make_uint4(0, 0, 0, 0);
+    auto load = [&](int tap, int c0) {
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+#pragma unroll
+        for (int i = 0; i < AS; ++i) {
+            const int zz = lz[i] + dz, yy = ly[i] + dy, xx = lx[i] + dx;
+            const bool in = lok[i] && zz >= 0 && zz < xa.d && yy >= 0 && yy < xa.h && xx >= 0 && xx < xa.w;
+            ra[i] = make_uint4(0, 0, 0, 0);
+            if (in) ra[i] = *reinterpret_cast<const uint4 *>(xb + (((int64_t)zz * xa.h + yy) * xa.w + xx) * xa.cstride + c0 + lh);
+        }
+        rb = make_uint4(0, 0, 0, 0);
+        if (bok) rb = *reinterpret_cast<const uint4 *>(wt + ((int64_t)bco * 27 + tap) * cin + c0 + lh);
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int i = 0; i < AS; ++i) *reinterpret_cast<uint4 *>(&As[buf][lr[i]][lh]) = ra[i];
+        if (bload) *reinterpret_cast<uint4 *>(&Bs[buf][br][lh]) = rb;
+    };
+    float acc[MT][NT][4] = {};
+    const int nck = cin / kCK, steps = 27 * nck;
+    int tap = 0, ck = 0;
+    load(0, 0);
+    store(0);
+    __syncthreads();
+    for (int s = 0; s < steps; ++s) {
+        const int cur = s & 1;
+        int ntap = tap, nc = ck + 1;
+        if (nc == nck) {
+            nc = 0;
+            ++ntap;
+        }
+        const bool more = s + 1 < steps;
+        if (more) load(ntap, nc * kCK);
+        warp_mma_tile<MT, NT>(As[cur], Bs[cur], warp * (BM / 4), acc);
+        if (more) store(cur ^ 1);
+        __syncthreads();
+        tap = ntap;
+        ck = nc;
+    }
+    // epilogue: rows warp * BM/4 + 16 m + grp (+8), columns co0 + 8 j + 2 tig (+1)
     const int lane = tid & 31, grp = lane >> 2, tig = lane & 3;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < NT; ++j) {
         const int co = co0 + j * 8 + tig * 2;
         if (co >= cout) continue;
         const float b0 = bias ? bias[co] : 0.0f, b1 = bias ? bias[co + 1] : 0.0f;
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const int64_t v = v0 + warp * 16 + grp + half * 8;
-            if (v >= nvox) continue;
-            float r0 = acc[j][half * 2] + b0, r1 = acc[j][half * 2 + 1] + b1;
-            if (relu) {
-                r0 = fmaxf(r0, 0.0f);
-                r1 = fmaxf(r1, 0.0f);
+        for (int m = 0; m < MT; ++m)
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const int64_t v = v0 + warp * (BM / 4) + m * 16 + grp + half * 8;
+                if (v >= nvox) continue;
+                float r0 = acc[m][j][half * 2] + b0, r1 = acc[m][j][half * 2 + 1] + b1;
+                if (relu) {
+                    r0 = fmaxf(r0, 0.0f);
+                    r1 = fmaxf(r1, 0.0f);
+                }
+                const int64_t o = ((int64_t)nb * nvox + v) * ya.cstride + ya.coff + co;
+                *reinterpret_cast<__nv_bfloat162 *>(y + o) = __floats2bfloat162_rn(r0, r1);
+                if (yf) {
+                    yf[o] = r0;
+                    yf[o + 1] = r1;
+                }
             }
-            const int64_t o = ((int64_t)nb * nvox + v) * ya.cstride + ya.coff + co;
-            *reinterpret_cast<__nv_bfloat162 *>(y + o) = __floats2bfloat162_rn(r0, r1);
-            if (yf) {
-                yf[o] = r0;
-                yf[o + 1] = r1;
-            }
-        }
     }
 }
 
@@ -470,9 +538,23 @@ int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *
         return fail(SRF_EINVAL, "conv3d needs Cin, Cout multiples of 16 and 16-byte aligned channel slices");
     if (xa.n != ya.n || xa.d != ya.d || xa.h != ya.h || xa.w != ya.w) return fail(SRF_EGRID, "x/y shapes differ");
     const int64_t nvox = (int64_t)xa.d * xa.h * xa.w;
-    dim3 grid((unsigned)((nvox + kCM - 1) / kCM), (unsigned)((cout + kCN - 1) / kCN), (unsigned)xa.n);
-    k_conv3d_fwd<<<grid, 128, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)x, xa, cin, (const __nv_bfloat16 *)w,
-                                                        bias, cout, relu, (__nv_bfloat16 *)y, ya, yf);
+    // the widest tile that still gives every SM two CTAs: 64 x 64 when Cout is a multiple of 64,
+    // else 128 voxels x 32 channels (no idle columns at Cout = 32 or 96), else 64 x 32
+    const int64_t fill = 2 * (int64_t)num_sms();
+    const auto ctas = [&](int bm, int bn) { return ((nvox + bm - 1) / bm) * ((cout + bn - 1) / bn) * xa.n; };
+    const __nv_bfloat16 *xp = (const __nv_bfloat16 *)x, *wp = (const __nv_bfloat16 *)w;
+    __nv_bfloat16 *yp = (__nv_bfloat16 *)y;
+    const cudaStream_t s = (cudaStream_t)stream;
+    if (cout % 64 == 0 && ctas(64, 64) >= fill) {
+        dim3 grid((unsigned)((nvox + 63) / 64), (unsigned)(cout / 64), (unsigned)xa.n);
+        k_conv3d_fwd<64, 64><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
+    } else if (ctas(128, 32) >= fill) {
+        dim3 grid((unsigned)((nvox + 127) / 128), (unsigned)((cout + 31) / 32), (unsigned)xa.n);
+        k_conv3d_fwd<128, 32><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
+    } else {
+        dim3 grid((unsigned)((nvox + 63) / 64), (unsigned)((cout + 31) / 32), (unsigned)xa.n);
+        k_conv3d_fwd<64, 32><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
+    }
     return check_cuda("conv3d forward launch");
 }
 
