@@ -297,65 +297,123 @@ __global__ void k_bias_grad(const __nv_bfloat16 *__restrict__ g, Act ga, int c, 
 }
 
 // 2x2x2 average pooling and its transpose; nearest 2x upsampling and its transpose
-__global__ void k_avgpool2(const __nv_bfloat16 *__restrict__ x, Act xa, __nv_bfloat16 *__restrict__ y, Act ya, int c) {
-    const int64_t total = (int64_t)ya.n * ya.d * ya.h * ya.w * c;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % c);
-        int64_t v = i / c;
-        const int ox = (int)(v % ya.w); v /= ya.w;
-        const int oy = (int)(v % ya.h); v /= ya.h;
-        const int oz = (int)(v % ya.d);
-        const int64_t nb = v / ya.d;
-        float s = 0.0f;
-        for (int k = 0; k < 8; ++k) {
-            const int zz = 2 * oz + (k >> 2), yy = 2 * oy + ((k >> 1) & 1), xx = 2 * ox + (k & 1);
-            if (zz < xa.d && yy < xa.h && xx < xa.w)
-                s += __bfloat162float(x[(((nb * xa.d + zz) * xa.h + yy) * xa.w + xx) * xa.cstride + xa.coff + ch]);
+// V consecutive channels as floats: 8 through one 16-byte access, or 1.
+template <int V>
+__device__ __forceinline__ void ld_ch(const __nv_bfloat16 *p, float (&f)[V]) {
+    if constexpr (V == 8) {
+        const uint4 u = *reinterpret_cast<const uint4 *>(p);
+        const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float2 t = __bfloat1622float2(h[i]);
+            f[2 * i] = t.x;
+            f[2 * i + 1] = t.y;
         }
-        y[(((nb * ya.d + oz) * ya.h + oy) * ya.w + ox) * ya.cstride + ya.coff + ch] = __float2bfloat16(0.125f * s);
+    } else {
+        f[0] = __bfloat162float(*p);
+    }
+}
+
+template <int V>
+__device__ __forceinline__ void st_ch(__nv_bfloat16 *p, const float (&f)[V]) {
+    if constexpr (V == 8) {
+        uint4 u;
+        __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&u);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+        *reinterpret_cast<uint4 *>(p) = u;
+    } else {
+        *p = __float2bfloat16(f[0]);
+    }
+}
+
+// Element i of a grid-stride loop over (voxel of `a`, group of V channels): the voxel's
+// coordinates and the group's first channel.
+struct VoxCh {
+    int64_t nb;
+    int z, y, x, ch;
+};
+__device__ __forceinline__ VoxCh vox_ch(int64_t i, const Act &a, int groups, int V) {
+    VoxCh r;
+    r.ch = (int)(i % groups) * V;
+    int64_t v = i / groups;
+    r.x = (int)(v % a.w);
+    v /= a.w;
+    r.y = (int)(v % a.h);
+    v /= a.h;
+    r.z = (int)(v % a.d);
+    r.nb = v / a.d;
+    return r;
+}
+
+__device__ __forceinline__ int64_t act_off(const Act &a, int64_t nb, int z, int y, int x, int ch) {
+    return (((nb * a.d + z) * a.h + y) * a.w + x) * a.cstride + a.coff + ch;
+}
+
+// y (coarse) = mean of the 8 children in x (fine), children outside the fine grid counting 0
+template <int V>
+__global__ void k_avgpool2(const __nv_bfloat16 *__restrict__ x, Act xa, __nv_bfloat16 *__restrict__ y, Act ya, int c) {
+    const int groups = c / V;
+    const int64_t total = (int64_t)ya.n * ya.d * ya.h * ya.w * groups;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const VoxCh o = vox_ch(i, ya, groups, V);
+        float s[V] = {};
+        for (int k = 0; k < 8; ++k) {
+            const int zz = 2 * o.z + (k >> 2), yy = 2 * o.y + ((k >> 1) & 1), xx = 2 * o.x + (k & 1);
+            if (zz < xa.d && yy < xa.h && xx < xa.w) {
+                float f[V];
+                ld_ch<V>(x + act_off(xa, o.nb, zz, yy, xx, o.ch), f);
+#pragma unroll
+                for (int q = 0; q < V; ++q) s[q] += f[q];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < V; ++q) s[q] *= 0.125f;
+        st_ch<V>(y + act_off(ya, o.nb, o.z, o.y, o.x, o.ch), s);
     }
 }
 
 // dx (fine) = dy (coarse) / 8 for the 8 children (the adjoint of k_avgpool2)
+template <int V>
 __global__ void k_avgpool2_bwd(const __nv_bfloat16 *__restrict__ dy, Act ya, __nv_bfloat16 *__restrict__ dx, Act xa, int c) {
-    const int64_t total = (int64_t)xa.n * xa.d * xa.h * xa.w * c;
+    const int groups = c / V;
+    const int64_t total = (int64_t)xa.n * xa.d * xa.h * xa.w * groups;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % c);
-        int64_t v = i / c;
-        const int xx = (int)(v % xa.w); v /= xa.w;
-        const int yy = (int)(v % xa.h); v /= xa.h;
-        const int zz = (int)(v % xa.d);
-        const int64_t nb = v / xa.d;
-        const int oz = zz / 2, oy = yy / 2, ox = xx / 2;
-        float g = 0.0f;
-        if (oz < ya.d && oy < ya.h && ox < ya.w)
-            g = 0.125f * __bfloat162float(dy[(((nb * ya.d + oz) * ya.h + oy) * ya.w + ox) * ya.cstride + ya.coff + ch]);
-        dx[(((nb * xa.d + zz) * xa.h + yy) * xa.w + xx) * xa.cstride + xa.coff + ch] = __float2bfloat16(g);
+        const VoxCh f = vox_ch(i, xa, groups, V);
+        const int oz = f.z / 2, oy = f.y / 2, ox = f.x / 2;
+        float g[V] = {};
+        if (oz < ya.d && oy < ya.h && ox < ya.w) {
+            ld_ch<V>(dy + act_off(ya, f.nb, oz, oy, ox, f.ch), g);
+#pragma unroll
+            for (int q = 0; q < V; ++q) g[q] *= 0.125f;
+        }
+        st_ch<V>(dx + act_off(xa, f.nb, f.z, f.y, f.x, f.ch), g);
     }
 }
 
 // y (fine) = x (coarse) at the parent voxel; mode 1: the adjoint (sum of the 8 children)
+template <int V>
 __global__ void k_upsample2(const __nv_bfloat16 *__restrict__ src, Act sa, __nv_bfloat16 *__restrict__ dst, Act da,
                             int c, int adjoint) {
-    const int64_t total = (int64_t)da.n * da.d * da.h * da.w * c;
+    const int groups = c / V;
+    const int64_t total = (int64_t)da.n * da.d * da.h * da.w * groups;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int ch = (int)(i % c);
-        int64_t v = i / c;
-        const int ox = (int)(v % da.w); v /= da.w;
-        const int oy = (int)(v % da.h); v /= da.h;
-        const int oz = (int)(v % da.d);
-        const int64_t nb = v / da.d;
-        float r = 0.0f;
+        const VoxCh o = vox_ch(i, da, groups, V);
+        float r[V] = {};
         if (!adjoint) {  // dst fine, src coarse
-            r = __bfloat162float(src[(((nb * sa.d + oz / 2) * sa.h + oy / 2) * sa.w + ox / 2) * sa.cstride + sa.coff + ch]);
+            ld_ch<V>(src + act_off(sa, o.nb, o.z / 2, o.y / 2, o.x / 2, o.ch), r);
         } else {  // dst coarse, src fine
             for (int k = 0; k < 8; ++k) {
-                const int zz = 2 * oz + (k >> 2), yy = 2 * oy + ((k >> 1) & 1), xx = 2 * ox + (k & 1);
-                if (zz < sa.d && yy < sa.h && xx < sa.w)
-                    r += __bfloat162float(src[(((nb * sa.d + zz) * sa.h + yy) * sa.w + xx) * sa.cstride + sa.coff + ch]);
+                const int zz = 2 * o.z + (k >> 2), yy = 2 * o.y + ((k >> 1) & 1), xx = 2 * o.x + (k & 1);
+                if (zz < sa.d && yy < sa.h && xx < sa.w) {
+                    float f[V];
+                    ld_ch<V>(src + act_off(sa, o.nb, zz, yy, xx, o.ch), f);
+#pragma unroll
+                    for (int q = 0; q < V; ++q) r[q] += f[q];
+                }
             }
         }
-        dst[(((nb * da.d + oz) * da.h + oy) * da.w + ox) * da.cstride + da.coff + ch] = __float2bfloat16(r);
+        st_ch<V>(dst + act_off(da, o.nb, o.z, o.y, o.x, o.ch), r);
     }
 }
 
@@ -522,6 +580,13 @@ inline int check_act(const Act &a, int c, const char *name) {
 
 inline Act act_of(const int32_t s[6]) { return Act{s[0], s[1], s[2], s[3], s[4], s[5]}; }
 
+// Both channel slices hold whole 16-byte groups of 8 channels (16-byte aligned buffers and
+// element offsets).
+inline bool vec8(const void *pa, const Act &a, const void *pb, const Act &b, int c) {
+    return c % 8 == 0 && a.cstride % 8 == 0 && a.coff % 8 == 0 && b.cstride % 8 == 0 && b.coff % 8 == 0 &&
+           (uintptr_t)pa % 16 == 0 && (uintptr_t)pb % 16 == 0;
+}
+
 }  // namespace srf
 
 using namespace srf;
@@ -615,12 +680,22 @@ int srf_cnn_pool2(const void *x, const int32_t xs[6], void *y, const int32_t ys[
     if (ya.d != (xa.d + 1) / 2 || ya.h != (xa.h + 1) / 2 || ya.w != (xa.w + 1) / 2 || xa.n != ya.n)
         return fail(SRF_EGRID, "coarse grid must be ceil(fine / 2)");
     cudaStream_t s = (cudaStream_t)stream;
-    if (!adjoint) {
+    const __nv_bfloat16 *xc = (const __nv_bfloat16 *)x, *yc = (const __nv_bfloat16 *)y;
+    __nv_bfloat16 *xm = (__nv_bfloat16 *)x, *ym = (__nv_bfloat16 *)y;
+    if (vec8(x, xa, y, ya, c)) {
+        if (!adjoint) {
+            const int64_t t = (int64_t)ya.n * ya.d * ya.h * ya.w * (c / 8);
+            k_avgpool2<8><<<grid_for(k_avgpool2<8>, t, 256), 256, 0, s>>>(xc, xa, ym, ya, c);
+        } else {
+            const int64_t t = (int64_t)xa.n * xa.d * xa.h * xa.w * (c / 8);
+            k_avgpool2_bwd<8><<<grid_for(k_avgpool2_bwd<8>, t, 256), 256, 0, s>>>(yc, ya, xm, xa, c);
+        }
+    } else if (!adjoint) {
         const int64_t t = (int64_t)ya.n * ya.d * ya.h * ya.w * c;
-        k_avgpool2<<<grid_for(k_avgpool2, t, 256), 256, 0, s>>>((const __nv_bfloat16 *)x, xa, (__nv_bfloat16 *)y, ya, c);
+        k_avgpool2<1><<<grid_for(k_avgpool2<1>, t, 256), 256, 0, s>>>(xc, xa, ym, ya, c);
     } else {  // y holds the coarse gradient, x receives the fine gradient
         const int64_t t = (int64_t)xa.n * xa.d * xa.h * xa.w * c;
-        k_avgpool2_bwd<<<grid_for(k_avgpool2_bwd, t, 256), 256, 0, s>>>((const __nv_bfloat16 *)y, ya, (__nv_bfloat16 *)x, xa, c);
+        k_avgpool2_bwd<1><<<grid_for(k_avgpool2_bwd<1>, t, 256), 256, 0, s>>>(yc, ya, xm, xa, c);
     }
     return check_cuda("pool launch");
 }
@@ -633,12 +708,21 @@ int srf_cnn_upsample2(const void *coarse, const int32_t cs[6], void *fine, const
     if (ca.d != (fa.d + 1) / 2 || ca.h != (fa.h + 1) / 2 || ca.w != (fa.w + 1) / 2 || ca.n != fa.n)
         return fail(SRF_EGRID, "coarse grid must be ceil(fine / 2)");
     cudaStream_t s = (cudaStream_t)stream;
+    const __nv_bfloat16 *cc = (const __nv_bfloat16 *)coarse, *fc = (const __nv_bfloat16 *)fine;
+    __nv_bfloat16 *cm = (__nv_bfloat16 *)coarse, *fm = (__nv_bfloat16 *)fine;
+    const bool v8 = vec8(coarse, ca, fine, fa, c);
     if (!adjoint) {
         const int64_t t = (int64_t)fa.n * fa.d * fa.h * fa.w * c;
-        k_upsample2<<<grid_for(k_upsample2, t, 256), 256, 0, s>>>((const __nv_bfloat16 *)coarse, ca, (__nv_bfloat16 *)fine, fa, c, 0);
+        if (v8)
+            k_upsample2<8><<<grid_for(k_upsample2<8>, t / 8, 256), 256, 0, s>>>(cc, ca, fm, fa, c, 0);
+        else
+            k_upsample2<1><<<grid_for(k_upsample2<1>, t, 256), 256, 0, s>>>(cc, ca, fm, fa, c, 0);
     } else {  // fine holds the gradient, coarse receives the sum over children
         const int64_t t = (int64_t)ca.n * ca.d * ca.h * ca.w * c;
-        k_upsample2<<<grid_for(k_upsample2, t, 256), 256, 0, s>>>((const __nv_bfloat16 *)fine, fa, (__nv_bfloat16 *)coarse, ca, c, 1);
+        if (v8)
+            k_upsample2<8><<<grid_for(k_upsample2<8>, t / 8, 256), 256, 0, s>>>(fc, fa, cm, ca, c, 1);
+        else
+            k_upsample2<1><<<grid_for(k_upsample2<1>, t, 256), 256, 0, s>>>(fc, fa, cm, ca, c, 1);
     }
     return check_cuda("upsample launch");
 }

@@ -1,34 +1,22 @@
 // Spot-check correction of the learned scatter estimate (not in the reference): a smooth
 // multiplicative correction fitted by least squares on the even spot-check SSS samples, judged on
-// the odd ones, and applied to the whole sinogram. The fit is one block (a k x k normal-equation
-// system in FP64, solved by Cholesky); the apply is one grid-stride pass. The estimate then reads
-// k + 2 numbers back, with no host arithmetic between its kernels.
+// the odd ones, and applied to the whole sinogram. The fit is one block: per-sample products in
+// FP32, summed by warp trees and then across warps in FP64, and the k x k normal equations
+// solved by Cholesky in FP64 (FP64 on the GPU only for these normalisation sums and the solve);
+// the apply is one grid-stride pass. The estimate then reads k + 2 numbers back, with no host
+// arithmetic between its kernels.
 #include "common.cuh"
 
 namespace srf {
 
 constexpr int kMaxBasis = 12;
-constexpr int kFitThreads = 256;
+constexpr int kFitThreads = 512;
 constexpr int kFitWarps = kFitThreads / 32;
 
-__device__ __forceinline__ double warp_sum_d(double v) {
+__device__ __forceinline__ float warp_sum_f(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
-}
-
-// Sums v over the block into every thread's return value; `scratch` holds kFitWarps doubles and
-// is free again when the function returns.
-__device__ __forceinline__ double block_sum_d(double v, double *scratch) {
-    v = warp_sum_d(v);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) scratch[w] = v;
-    __syncthreads();
-    double t = 0.0;
-#pragma unroll
-    for (int i = 0; i < kFitWarps; ++i) t += scratch[i];
-    __syncthreads();
-    return t;
 }
 
 template <int K>
@@ -38,55 +26,57 @@ k_spot_fit(const float *__restrict__ pred, int64_t nbins, const int64_t *__restr
            float *__restrict__ out) {
     constexpr int NG = K * (K + 1) / 2;  // packed upper triangle of the normal matrix
     constexpr int NS = NG + K;           // and the right-hand side
-    __shared__ double scratch[kFitWarps];
-    __shared__ double part[kFitWarps][NS];
+    __shared__ float part[kFitWarps][NS];
+    __shared__ float part3[kFitWarps][3];
     __shared__ double ata[K][K], atb[K], beta[K];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // normal equations over the even samples: a_j = pred * phi_j. A sample whose bin lies
     // outside [0, nbins) is left out (the odd pass below does the same).
-    double g[NS];
+    float g[NS];
 #pragma unroll
-    for (int e = 0; e < NS; ++e) g[e] = 0.0;
+    for (int e = 0; e < NS; ++e) g[e] = 0.0f;
     for (int s = 2 * threadIdx.x; s < n; s += 2 * kFitThreads) {
         const int64_t b = bins[s];
         if ((uint64_t)b >= (uint64_t)nbins) continue;
-        const double p = (double)pred[b], y = (double)ref[s];
-        double a[K];
+        const float p = pred[b], y = ref[s];
+        float a[K];
 #pragma unroll
-        for (int j = 0; j < K; ++j) a[j] = p * (double)phi[j * nbins + b];
+        for (int j = 0; j < K; ++j) a[j] = p * phi[j * nbins + b];
         int e = 0;
 #pragma unroll
         for (int j = 0; j < K; ++j) {
 #pragma unroll
             for (int l = j; l < K; ++l) {
-                g[e] = fma(a[j], a[l], g[e]);
+                g[e] = fmaf(a[j], a[l], g[e]);
                 ++e;
             }
         }
 #pragma unroll
-        for (int j = 0; j < K; ++j) g[NG + j] = fma(a[j], y, g[NG + j]);
+        for (int j = 0; j < K; ++j) g[NG + j] = fmaf(a[j], y, g[NG + j]);
     }
-    {
-        const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
 #pragma unroll
-        for (int e = 0; e < NS; ++e) {
-            const double v = warp_sum_d(g[e]);
-            if (l == 0) part[w][e] = v;
+    for (int e = 0; e < NS; ++e) {
+        const float v = warp_sum_f(g[e]);
+        if (lane == 0) part[w][e] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NS) {  // entry e = threadIdx.x: (j, l) of the packed triangle, or rhs j
+        double v = 0.0;
+        for (int i = 0; i < kFitWarps; ++i) v += (double)part[i][threadIdx.x];
+        int e = threadIdx.x;
+        if (e >= NG) {
+            atb[e - NG] = v;
+        } else {
+            int j = 0;
+            while (e >= K - j) {
+                e -= K - j;
+                ++j;
+            }
+            ata[j][j + e] = ata[j + e][j] = v;
         }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        int e = 0;
-        for (int j = 0; j < K; ++j)
-            for (int l = j; l < K; ++l, ++e) {
-                double v = 0.0;
-                for (int w = 0; w < kFitWarps; ++w) v += part[w][e];
-                ata[j][l] = ata[l][j] = v;
-            }
-        for (int j = 0; j < K; ++j) {
-            double v = 0.0;
-            for (int w = 0; w < kFitWarps; ++w) v += part[w][NG + j];
-            atb[j] = v;
-        }
         double tr = 0.0;
         for (int j = 0; j < K; ++j) tr += ata[j][j];
         int okay = tr > 0.0 && isfinite(tr);
@@ -108,14 +98,13 @@ k_spot_fit(const float *__restrict__ pred, int64_t nbins, const int64_t *__restr
             }
         }
         if (okay) {
-            double z[K];
-            for (int i = 0; i < K; ++i) {
+            for (int i = 0; i < K; ++i) {  // L z = atb, z kept in atb
                 double v = atb[i];
-                for (int m = 0; m < i; ++m) v -= ata[i][m] * z[m];
-                z[i] = v / ata[i][i];
+                for (int m = 0; m < i; ++m) v -= ata[i][m] * atb[m];
+                atb[i] = v / ata[i][i];
             }
-            for (int i = K - 1; i >= 0; --i) {
-                double v = z[i];
+            for (int i = K - 1; i >= 0; --i) {  // L^T beta = z
+                double v = atb[i];
                 for (int m = i + 1; m < K; ++m) v -= ata[m][i] * beta[m];
                 beta[i] = v / ata[i][i];
             }
@@ -125,27 +114,42 @@ k_spot_fit(const float *__restrict__ pred, int64_t nbins, const int64_t *__restr
     }
     __syncthreads();
     // judged on the odd samples, which the fit has not seen
-    double e2 = 0.0, u2 = 0.0, y2 = 0.0;
+    float bf[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) bf[j] = (float)beta[j];
+    float e2 = 0.0f, u2 = 0.0f, y2 = 0.0f;
     for (int s = 2 * threadIdx.x + 1; s < n; s += 2 * kFitThreads) {
         const int64_t b = bins[s];
         if ((uint64_t)b >= (uint64_t)nbins) continue;
-        const double p = (double)pred[b], y = (double)ref[s];
-        double c = 0.0;
+        const float p = pred[b], y = ref[s];
+        float c = 0.0f;
 #pragma unroll
-        for (int j = 0; j < K; ++j) c = fma(beta[j], (double)phi[j * nbins + b], c);
-        const double d = p * c - y, u = p - y;
-        e2 = fma(d, d, e2);
-        u2 = fma(u, u, u2);
-        y2 = fma(y, y, y2);
+        for (int j = 0; j < K; ++j) c = fmaf(bf[j], phi[j * nbins + b], c);
+        const float d = fmaf(p, c, -y), u = p - y;
+        e2 = fmaf(d, d, e2);
+        u2 = fmaf(u, u, u2);
+        y2 = fmaf(y, y, y2);
     }
-    e2 = block_sum_d(e2, scratch);
-    u2 = block_sum_d(u2, scratch);
-    y2 = block_sum_d(y2, scratch);
+    e2 = warp_sum_f(e2);
+    u2 = warp_sum_f(u2);
+    y2 = warp_sum_f(y2);
+    if (lane == 0) {
+        part3[w][0] = e2;
+        part3[w][1] = u2;
+        part3[w][2] = y2;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        const double den = sqrt(fmax(y2, 1e-60));
+        double se = 0.0, su = 0.0, sy = 0.0;
+        for (int i = 0; i < kFitWarps; ++i) {
+            se += (double)part3[i][0];
+            su += (double)part3[i][1];
+            sy += (double)part3[i][2];
+        }
+        const double den = sqrt(fmax(sy, 1e-60));
         for (int j = 0; j < K; ++j) out[j] = (float)beta[j];
-        out[K] = (float)(sqrt(e2) / den);
-        out[K + 1] = (float)(sqrt(u2) / den);
+        out[K] = (float)(sqrt(se) / den);
+        out[K + 1] = (float)(sqrt(su) / den);
     }
 }
 

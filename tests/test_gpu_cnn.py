@@ -66,28 +66,41 @@ def test_conv_forward_dgrad_wgrad(cuda_lib, cnn):
 
 
 def test_pool_upsample_and_adjoints(cuda_lib, cnn):
+    """Pooling, upsampling and their adjoints against the oracle, on whole 16-channel buffers (the
+    8-channel vector path) and on a 12-channel slice at channel offset 4 (the scalar path); the
+    channels outside the slice stay untouched."""
     from srf_gb300._lib import call, i32, ptr, stream_ptr
     from srf_gb300.surrogate import act
     rng = np.random.default_rng(1)
     dev = torch.device("cuda", 0)
     fine = (2, 5, 6, 7, 16)
     coarse = (2, 3, 3, 4, 16)
-    # multiples of 1/8 with small numerators are exact in bfloat16 and in the sums below
-    x = _bf(rng.integers(-8, 8, fine) / 8.0).to(dev)
-    c = torch.zeros(coarse, dtype=torch.bfloat16, device=dev)
     s = stream_ptr(dev)
-    call("srf_cnn_pool2", ptr(x), act(x), ptr(c), act(c), i32(16), i32(0), s)
-    assert np.allclose(_np(c), cnn.pool2(_np(x)), atol=1e-2)
-    g = _bf(rng.integers(-8, 8, coarse)).to(dev)
-    gx = torch.zeros(fine, dtype=torch.bfloat16, device=dev)
-    call("srf_cnn_pool2", ptr(gx), act(gx), ptr(g), act(g), i32(16), i32(1), s)
-    assert np.array_equal(_np(gx), cnn.pool2_adjoint(_np(g), fine))
-    u = torch.zeros(fine, dtype=torch.bfloat16, device=dev)
-    call("srf_cnn_upsample2", ptr(g), act(g), ptr(u), act(u), i32(16), i32(0), s)
-    assert np.array_equal(_np(u), cnn.upsample2(_np(g), fine))
-    gc = torch.zeros(coarse, dtype=torch.bfloat16, device=dev)
-    call("srf_cnn_upsample2", ptr(gc), act(gc), ptr(x), act(x), i32(16), i32(1), s)
-    assert np.allclose(_np(gc), cnn.upsample2_adjoint(_np(x), coarse), atol=1e-2)
+    for c, off in ((16, 0), (12, 4)):
+        sl = slice(off, off + c)
+        # multiples of 1/8 with small numerators are exact in bfloat16 and in the sums below
+        x = _bf(rng.integers(-8, 8, fine) / 8.0).to(dev)
+        cb = torch.zeros(coarse, dtype=torch.bfloat16, device=dev)
+        call("srf_cnn_pool2", ptr(x), act(x, off), ptr(cb), act(cb, off), i32(c), i32(0), s)
+        got = _np(cb)
+        assert np.allclose(got[..., sl], cnn.pool2(_np(x)[..., sl]), atol=1e-2)
+        assert not got[..., :off].any()
+        g = _bf(rng.integers(-8, 8, coarse)).to(dev)
+        gx = torch.zeros(fine, dtype=torch.bfloat16, device=dev)
+        call("srf_cnn_pool2", ptr(gx), act(gx, off), ptr(g), act(g, off), i32(c), i32(1), s)
+        got = _np(gx)
+        assert np.array_equal(got[..., sl], cnn.pool2_adjoint(_np(g)[..., sl], fine[:4] + (c,)))
+        assert not got[..., :off].any()
+        u = torch.zeros(fine, dtype=torch.bfloat16, device=dev)
+        call("srf_cnn_upsample2", ptr(g), act(g, off), ptr(u), act(u, off), i32(c), i32(0), s)
+        got = _np(u)
+        assert np.array_equal(got[..., sl], cnn.upsample2(_np(g)[..., sl], fine[:4] + (c,)))
+        assert not got[..., :off].any()
+        gc = torch.zeros(coarse, dtype=torch.bfloat16, device=dev)
+        call("srf_cnn_upsample2", ptr(gc), act(gc, off), ptr(x), act(x, off), i32(c), i32(1), s)
+        got = _np(gc)
+        assert np.allclose(got[..., sl], cnn.upsample2_adjoint(_np(x)[..., sl], coarse[:4] + (c,)), atol=1e-2)
+        assert not got[..., :off].any()
 
 
 def test_head8_forward_and_gradients(cuda_lib, cnn):
