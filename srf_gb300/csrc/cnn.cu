@@ -190,6 +190,127 @@ k_conv3d_fwd(const __nv_bfloat16 *__restrict__ x, Act xa, int cin, const __nv_bf
     }
 }
 
+// Small grids (too few CTAs to hide the latency of a long chain of K steps): each of the 4 warps
+// walks every 4th (tap, 16-channel) step of the whole 64-voxel x 32-channel tile through its own
+// double buffer, synchronising only within the warp; the four partial tiles are then summed
+// through shared memory (reusing the buffers) and written with the bias and activation.
+constexpr int kWsM = 64, kWsN = 32, kWsRed = 36;  // reduction row stride (floats)
+constexpr int kWsWarpBytes = (2 * kWsM + 2 * kWsN) * kCPad * 2;
+static_assert(4 * kWsM * kWsRed * 4 <= 4 * kWsWarpBytes, "reduction fits in the staging buffers");
+
+__global__ void __launch_bounds__(128)
+k_conv3d_fwd_wsplit(const __nv_bfloat16 *__restrict__ x, Act xa, int cin, const __nv_bfloat16 *__restrict__ wt,
+                    const float *__restrict__ bias, int cout, int relu, __nv_bfloat16 *__restrict__ y, Act ya,
+                    float *__restrict__ yf) {
+    __shared__ __align__(16) unsigned char smem[4 * kWsWarpBytes];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    typedef __nv_bfloat16 ARow[kCPad];
+    ARow *As = reinterpret_cast<ARow *>(smem + warp * kWsWarpBytes);  // [2][kWsM]
+    ARow *Bs = As + 2 * kWsM;                                          // [2][kWsN]
+    const int64_t nvox = (int64_t)xa.d * xa.h * xa.w;
+    const int64_t v0 = (int64_t)blockIdx.x * kWsM;
+    const int co0 = blockIdx.y * kWsN;
+    const int nb = blockIdx.z;
+    const __nv_bfloat16 *xb = x + (int64_t)nb * nvox * xa.cstride + xa.coff;
+    // lane slots: A rows lane / 2 + 16 i (i < 4), B rows lane / 2 + 16 i (i < 2), half (lane & 1) * 8
+    const int lh = (lane & 1) * 8, r0 = lane >> 1;
+    int lz[4], ly[4], lx[4];
+    bool lok[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t v = v0 + r0 + 16 * i;
+        lok[i] = v < nvox;
+        const int z = lok[i] ? (int)(v / ((int64_t)xa.h * xa.w)) : 0;
+        const int rem = lok[i] ? (int)(v - (int64_t)z * xa.h * xa.w) : 0;
+        lz[i] = z;
+        ly[i] = rem / xa.w;
+        lx[i] = rem - ly[i] * xa.w;
+    }
+    uint4 ra[4], rb[2];
+    const int nck = cin / kCK, steps = 27 * nck;
+    auto load = [&](int st) {
+        const int tap = st / nck, c0 = (st - tap * nck) * kCK;
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int zz = lz[i] + dz, yy = ly[i] + dy, xx = lx[i] + dx;
+            const bool in = lok[i] && zz >= 0 && zz < xa.d && yy >= 0 && yy < xa.h && xx >= 0 && xx < xa.w;
+            ra[i] = make_uint4(0, 0, 0, 0);
+            if (in) ra[i] = *reinterpret_cast<const uint4 *>(xb + (((int64_t)zz * xa.h + yy) * xa.w + xx) * xa.cstride + c0 + lh);
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const int co = co0 + r0 + 16 * i;
+            rb[i] = make_uint4(0, 0, 0, 0);
+            if (co < cout) rb[i] = *reinterpret_cast<const uint4 *>(wt + ((int64_t)co * 27 + tap) * cin + c0 + lh);
+        }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) *reinterpret_cast<uint4 *>(&As[buf * kWsM + r0 + 16 * i][lh]) = ra[i];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) *reinterpret_cast<uint4 *>(&Bs[buf * kWsN + r0 + 16 * i][lh]) = rb[i];
+    };
+    float acc[4][4][4] = {};
+    if (warp < steps) {
+        load(warp);
+        store(0);
+    }
+    __syncwarp();
+    int it = 0;
+    for (int st = warp; st < steps; st += 4, ++it) {
+        const int cur = it & 1;
+        const bool more = st + 4 < steps;
+        if (more) load(st + 4);
+        warp_mma_tile<4, 4>(As + cur * kWsM, Bs + cur * kWsN, 0, acc);
+        if (more) store(cur ^ 1);
+        __syncwarp();
+    }
+    __syncthreads();  // every warp is done with its staging buffers
+    float *red = reinterpret_cast<float *>(smem) + warp * kWsM * kWsRed;
+    const int grp = lane >> 2, tig = lane & 3;
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const int r = m * 16 + grp + half * 8, c = j * 8 + tig * 2;
+                *reinterpret_cast<float2 *>(&red[r * kWsRed + c]) =
+                    make_float2(acc[m][j][half * 2], acc[m][j][half * 2 + 1]);
+            }
+    __syncthreads();
+    // thread t: column pair t % 16, rows t / 16 + 8 k
+    const float *red0 = reinterpret_cast<const float *>(smem);
+    const int cp = (tid & 15) * 2, co = co0 + cp;
+    if (co < cout) {
+        const float b0 = bias ? bias[co] : 0.0f, b1 = bias ? bias[co + 1] : 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int r = (tid >> 4) + 8 * k;
+            const int64_t v = v0 + r;
+            if (v >= nvox) continue;
+            float s0 = b0, s1 = b1;
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+                const float2 p = *reinterpret_cast<const float2 *>(&red0[(w * kWsM + r) * kWsRed + cp]);
+                s0 += p.x;
+                s1 += p.y;
+            }
+            if (relu) {
+                s0 = fmaxf(s0, 0.0f);
+                s1 = fmaxf(s1, 0.0f);
+            }
+            const int64_t o = ((int64_t)nb * nvox + v) * ya.cstride + ya.coff + co;
+            *reinterpret_cast<__nv_bfloat162 *>(y + o) = __floats2bfloat162_rn(s0, s1);
+            if (yf) {
+                yf[o] = s0;
+                yf[o + 1] = s1;
+            }
+        }
+    }
+}
+
 // dw[co, tap, ci] += sum_v dy[v, co] x[v + tap - 1, ci]; grid (voxel splits, 27 taps, co/ci tiles)
 __global__ void __launch_bounds__(128)
 k_conv3d_wgrad(const __nv_bfloat16 *__restrict__ x, Act xa, int cin, const __nv_bfloat16 *__restrict__ dy,
@@ -604,7 +725,8 @@ int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *
     if (xa.n != ya.n || xa.d != ya.d || xa.h != ya.h || xa.w != ya.w) return fail(SRF_EGRID, "x/y shapes differ");
     const int64_t nvox = (int64_t)xa.d * xa.h * xa.w;
     // the widest tile that still gives every SM two CTAs: 64 x 64 when Cout is a multiple of 64,
-    // else 128 voxels x 32 channels (no idle columns at Cout = 32 or 96), else 64 x 32
+    // else 128 voxels x 32 channels (no idle columns at Cout = 32 or 96); below that, 64 x 32
+    // tiles with K split over each CTA's warps
     const int64_t fill = 2 * (int64_t)num_sms();
     const auto ctas = [&](int bm, int bn) { return ((nvox + bm - 1) / bm) * ((cout + bn - 1) / bn) * xa.n; };
     const __nv_bfloat16 *xp = (const __nv_bfloat16 *)x, *wp = (const __nv_bfloat16 *)w;
@@ -616,9 +738,9 @@ int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *
     } else if (ctas(128, 32) >= fill) {
         dim3 grid((unsigned)((nvox + 127) / 128), (unsigned)((cout + 31) / 32), (unsigned)xa.n);
         k_conv3d_fwd<128, 32><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
-    } else {
-        dim3 grid((unsigned)((nvox + 63) / 64), (unsigned)((cout + 31) / 32), (unsigned)xa.n);
-        k_conv3d_fwd<64, 32><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
+    } else {  // too few CTAs to hide a long K chain: split K over the warps of each CTA
+        dim3 grid((unsigned)((nvox + kWsM - 1) / kWsM), (unsigned)((cout + kWsN - 1) / kWsN), (unsigned)xa.n);
+        k_conv3d_fwd_wsplit<<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
     }
     return check_cuda("conv3d forward launch");
 }

@@ -65,6 +65,28 @@ def test_conv_forward_dgrad_wgrad(cuda_lib, cnn):
     assert rel_l2(dw.cpu().numpy(), cnn.conv3d_wgrad(x64, _np(dy))) <= 1e-5
 
 
+def test_conv_forward_tile_shapes(cuda_lib, cnn):
+    """srf_conv3d_fwd picks its tile from the grid it is given: grids large enough for 64 x 64
+    tiles (Cout = 64) and for 128 x 32 tiles (Cout = 32) against the oracle (the small grid of the
+    test above takes the split-K tile)."""
+    from srf_gb300._lib import call, i32, ptr, stream_ptr
+    from srf_gb300.surrogate import act
+    rng = np.random.default_rng(5)
+    dev = torch.device("cuda", 0)
+    s = stream_ptr(dev)
+    for shape, cin, cout in (((1, 13, 40, 40), 32, 64), ((1, 25, 40, 40), 16, 32)):
+        x = _bf(rng.standard_normal(shape + (cin,))).to(dev)
+        wt = _bf(rng.standard_normal((cout, 27, cin)) * 0.1).to(dev)
+        bias = torch.as_tensor(rng.standard_normal(cout).astype(np.float32)).to(dev)
+        y = torch.zeros(shape + (cout,), dtype=torch.bfloat16, device=dev)
+        yf = torch.zeros(shape + (cout,), dtype=torch.float32, device=dev)
+        call("srf_conv3d_fwd", ptr(x), act(x), i32(cin), ptr(wt), ptr(bias), i32(cout), i32(1), ptr(y),
+             act(y), ptr(yf), s)
+        ref = cnn.conv3d(_np(x), _np(wt), bias.cpu().numpy(), relu=True)
+        assert rel_l2(yf.cpu().numpy(), ref) <= 1e-5, (shape, cin, cout)
+        assert rel_l2(_np(y), ref) <= 4e-3
+
+
 def test_pool_upsample_and_adjoints(cuda_lib, cnn):
     """Pooling, upsampling and their adjoints against the oracle, on whole 16-channel buffers (the
     8-channel vector path) and on a 12-channel slice at channel offset 4 (the scalar path); the
