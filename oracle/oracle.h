@@ -2,7 +2,8 @@
  *
  * A plain-C restatement of srfnef's Siddon projector / backprojector (non-TOF and TOF) and of its
  * single-scatter simulation, used by tests/, by __graft_entry__.smoke() and by bench.py's CPU
- * baseline leg as the checker. The product (srf_gb300/) never links, loads or calls it.
+ * baseline leg, as the reference the GPU results are compared with. The product (srf_gb300/)
+ * never links, loads or calls it.
  *
  * Parity pin: siddon_oracle.c is checked bit-for-bit against the reference's own device functions
  * compiled on the host (oracle/_ref, see Makefile) and against the committed golden vectors

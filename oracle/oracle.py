@@ -1,7 +1,8 @@
 """CPU oracle for the list-mode reconstruction hot path. TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this module, and
-only as the checker. The product package srf_gb300 never imports it.
+only as the reference the GPU results are compared with. The product package srf_gb300 never
+imports it.
 
 * ``projection`` / ``backprojection`` / ``projection_adjoint`` -- ctypes bindings of the C
   restatement in siddon_oracle.c (built by ``make -C oracle`` into oracle/_build/liboracle.so);

@@ -15,7 +15,7 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def oracle():
-    import oracle as O  # the CPU checker (oracle/oracle.py)
+    import oracle as O  # the CPU oracle (oracle/oracle.py)
     O.build()
     return O
 
