@@ -7,13 +7,15 @@
 // live in the optimiser.
 //
 // conv3d 3x3x3 (pad 1, stride 1) is an implicit GEMM: rows = output voxels, columns = output
-// channels, K = 27 taps x Cin. A CTA of 4 warps computes a 64-voxel x 64-channel tile; for each
-// (tap, 16-channel chunk) the gathered input rows (zero outside the volume) and the weight slice
-// are staged in shared memory and each warp issues 8 mma.sync.m16n8k16 BF16 tensor-core
-// products into FP32 accumulators. The data gradient is the same kernel on flipped, transposed
-// weights. The weight gradient is a split-K GEMM over voxels per tap, accumulated with FP32
-// atomics. Requirements (checked on the host): Cin and Cout multiples of 16, channel strides and
-// offsets multiples of 8 (16-byte aligned rows).
+// channels, K = 27 taps x Cin, walked in (tap, 16-channel chunk) steps. For each step the
+// gathered input rows (zero outside the volume) and the weight slice are staged in shared memory
+// and the warps issue mma.sync.m16n8k16 BF16 tensor-core products into FP32 accumulators. The
+// tile follows the layer: 64 voxels x 64 channels or 128 x 32 when the grid fills the GPU
+// (double-buffered, one barrier per step), else 64 x 32 with the K steps dealt round-robin to the
+// CTA's 4 warps and their partial tiles summed at the end. The data gradient is the same kernel
+// on flipped, transposed weights. The weight gradient is a split-K GEMM over voxels per tap,
+// accumulated with FP32 atomics. Requirements (checked on the host): Cin and Cout multiples of
+// 16, channel strides and offsets multiples of 8 (16-byte aligned rows).
 #include <algorithm>
 #include <cuda_bf16.h>
 
