@@ -1,8 +1,9 @@
-// Projector family entry points: forward projection, backprojection and the exact adjoint (non-TOF
-// and TOF, single image or batched; these run on the fused kernel's traversal in osem.cu), visit
-// counts, attenuation, and the view fold/copy helpers. k_trace here is grid-stride over LORs with G
-// lanes per LOR and the per-slab setup of siddon.cuh; it serves the visit counts and the
-// allocation-free TOF backprojection.
+// Projector family entry points: forward projection and backprojection (non-TOF and TOF; these run
+// on the fused kernel's traversal in osem.cu), the exact adjoint (batched: the fused traversal;
+// single image: k_trace, which measured faster there than the batched kernel with one image),
+// visit counts, attenuation, and the view fold/copy helpers. k_trace here is grid-stride over LORs
+// with G lanes per LOR and the per-slab setup of siddon.cuh; it also serves the visit counts and
+// the allocation-free TOF backprojection.
 #include "common.cuh"
 #include "fused.cuh"
 
@@ -209,10 +210,10 @@ int srf_projection_adjoint(const float *lors, int64_t n, int32_t lor_stride, con
     if (tof) {
         TofParams tp;
         if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
-        return fused_adjoint_batch(lors, n, lor_stride, tof, tof_stride, g, tp, 1, 0, values, n, v, vt, (cudaStream_t)stream);
+        return launch_trace<true, RULES_PROJ, SCATTER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
     }
     TofParams tp{0, 0, 0};
-    return fused_adjoint_batch(lors, n, lor_stride, nullptr, 1, g, tp, 1, 0, values, n, v, vt, (cudaStream_t)stream);
+    return launch_trace<false, RULES_PROJ, SCATTER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
 }
 
 static int batch_args(int32_t n_images, int64_t batch_stride, int64_t row_stride, int64_t n,
