@@ -78,6 +78,26 @@ def test_argument_checks(lib):
     assert b"ratio" in lib.srf_last_error()
     # empty input succeeds without a launch
     assert p(None, ctypes.c_int64(0), 6, fake, st, None, None, grid, center, size, None, None) == 0
+    # surrogate spot check: basis size, sample count, ridge, NULL pointers
+    fit = lib.srf_spot_fit
+    i64, i32, f64 = ctypes.c_int64, ctypes.c_int32, ctypes.c_double
+    assert fit(fake, i64(100), fake, fake, i32(64), fake, i32(13), f64(1e-6), fake, None) == 1
+    assert fit(fake, i64(100), fake, fake, i32(1), fake, i32(9), f64(1e-6), fake, None) == 1
+    assert fit(fake, i64(100), fake, fake, i32(64), fake, i32(9), f64(-1.0), fake, None) == 1
+    assert fit(fake, i64(100), None, fake, i32(64), fake, i32(9), f64(1e-6), fake, None) == 1
+    sb = lib.srf_scale_by_basis
+    assert sb(fake, i64(100), fake, i32(0), fake, None) == 1
+    assert sb(fake, i64(100), None, i32(9), fake, None) == 1
+    assert sb(fake, i64(0), fake, i32(9), fake, None) == 0
+    # convolution: channel counts not multiples of 16, a slice past the channel stride, shapes that differ
+    a6 = lambda *v: (ctypes.c_int32 * 6)(*v)
+    conv = lib.srf_conv3d_fwd
+    assert conv(fake, a6(1, 4, 4, 4, 16, 0), i32(12), fake, None, i32(16), i32(1), fake, a6(1, 4, 4, 4, 16, 0),
+                None, None) == 1
+    assert conv(fake, a6(1, 4, 4, 4, 16, 8), i32(16), fake, None, i32(16), i32(1), fake, a6(1, 4, 4, 4, 16, 0),
+                None, None) == 2
+    assert conv(fake, a6(1, 4, 4, 4, 16, 0), i32(16), fake, None, i32(16), i32(1), fake, a6(1, 4, 4, 5, 16, 0),
+                None, None) == 2
 
 
 def test_study_descriptor_layout_matches_header(tmp_path):
