@@ -1,6 +1,7 @@
 // Shared host-side plumbing of the C ABI: status codes, per-thread error text, argument checks,
 // launch sizing.
 #pragma once
+#include <atomic>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -46,14 +47,16 @@ inline int num_sms() {
     return cached;
 }
 
-inline int &group_lanes() {
-    static int lanes = 32;
+// Process-wide tuning knobs (srf_set_tuning): atomic, so a setter on one host thread does not race
+// with launches reading them on others. Lanes per LOR of the traversal kernels (8, 16 or 32).
+inline std::atomic<int> &group_lanes() {
+    static std::atomic<int> lanes{32};
     return lanes;
 }
 
 // Slabs each lane of a LOR group handles per chunk in the fused OSEM kernel (2 or 4; default 4).
-inline int &slabs_per_lane() {
-    static int u = 4;
+inline std::atomic<int> &slabs_per_lane() {
+    static std::atomic<int> u{4};
     return u;
 }
 
@@ -63,13 +66,9 @@ constexpr int kBlock = 256;
 // fill every SM to its occupancy limit, never more than the work needs.
 template <typename K>
 inline unsigned grid_for(K kernel, int64_t units, int per_block, int smem = 0, int block = kBlock) {
-    static thread_local int cache_dev = -1;
-    int dev = 0;
-    cudaGetDevice(&dev);
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, block, smem);
     if (occ < 1) occ = 1;
-    (void)cache_dev;
     int64_t need = (units + per_block - 1) / per_block;
     int64_t cap = (int64_t)num_sms() * occ;
     int64_t g = need < cap ? need : cap;
