@@ -296,6 +296,8 @@ def spot_fit(pred: torch.Tensor, bins: torch.Tensor, ref: torch.Tensor, basis: t
     k, nb = basis.shape
     assert pred.dtype == F32 and ref.dtype == F32 and basis.dtype == F32 and bins.dtype == torch.int64
     assert pred.numel() == nb and out.numel() >= k + 2 and bins.numel() == ref.numel()
+    assert all(t.is_cuda and t.is_contiguous() for t in (pred, bins, ref, basis, out)), \
+        "spot_fit takes contiguous CUDA tensors"
     call("srf_spot_fit", ptr(pred), i64(nb), ptr(bins), ptr(ref), i32(bins.numel()), ptr(basis), i32(k),
          f64(ridge), ptr(out), stream_ptr(pred.device))
 
@@ -304,6 +306,8 @@ def scale_by_basis(x: torch.Tensor, basis: torch.Tensor, beta: torch.Tensor) -> 
     """srf_scale_by_basis: x *= beta . basis, in place (beta on the device)."""
     k, nb = basis.shape
     assert x.dtype == F32 and x.numel() == nb and beta.numel() >= k
+    assert all(t.is_cuda and t.is_contiguous() for t in (x, basis, beta)), \
+        "scale_by_basis takes contiguous CUDA tensors"
     call("srf_scale_by_basis", ptr(x), i64(nb), ptr(basis), i32(k), ptr(beta), stream_ptr(x.device))
 
 
