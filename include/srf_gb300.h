@@ -101,7 +101,9 @@ int srf_backprojection_tof(const float *lors, int64_t n, int32_t lor_stride,
  * that loads the library) and folded into `image` (x-fastest, strides {1, nx, nx*ny}), which is
  * accumulated into like srf_backprojection_tof. Grids with more voxels return SRF_ERANGE. The first
  * call on a device looks up the array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture. All calls share the array: calls that overlap on the GPU race. */
+ * before any stream capture. The address is cached per device ordinal for the process, which
+ * assumes the runtime's primary context: no cudaDeviceReset and no second driver-API context on the
+ * device afterwards. All calls share the array: calls that overlap on the GPU race. */
 #define SRF_NOALLOC_MAX_VOXELS 4718592
 int srf_backprojection_tof_noalloc(const float *lors, int64_t n, int32_t lor_stride,
                                    const float *tof, int32_t tof_stride,

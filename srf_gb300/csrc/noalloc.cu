@@ -11,14 +11,20 @@
 // The array holds SRF_NOALLOC_MAX_VOXELS floats (18 MiB); every GPU that loads the library holds
 // it until the process exits. All calls share it: calls that overlap on the GPU (different
 // streams, or other threads) race on it and must be serialised by the caller.
+//
+// The traversal is srf_backprojection_tof's own (fused_backprojection), with the static array as
+// its y-fastest accumulator, so the two entry points compute the same thing the same way.
+//
+// The array's device address is looked up once per device ordinal and cached for the life of
+// the process. That assumes the CUDA runtime's primary context of each device: after
+// cudaDeviceReset, or from a second context that the driver API made current on the same device,
+// the cached address would no longer be this context's copy of the array.
 #include <mutex>
 
 #include "common.cuh"
+#include "fused.cuh"
 
 namespace srf {
-int backprojection_tof_views(const float *lors, int64_t n, int stride, const float *tof,
-                             int tof_stride, const Grid &g, const TofParams &tp, const View &v,
-                             const View &vt, const float *values, cudaStream_t s);
 int fold_views(float *dst, const View &d, const float *src, const View &sv, const Grid &g,
                cudaStream_t s);
 }  // namespace srf
@@ -80,6 +86,6 @@ extern "C" int srf_backprojection_tof_noalloc(const float *lors, int64_t n, int3
     if (e != cudaSuccess) return fail(SRF_ECUDA, "clearing scratch: %s", cudaGetErrorString(e));
     View v{image, {1, g.nx, (int64_t)g.nx * g.ny}};
     View vt{scratch, {g.ny, 1, (int64_t)g.nx * g.ny}};
-    if ((rc = backprojection_tof_views(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, values, s))) return rc;
+    if ((rc = fused_backprojection(lors, n, lor_stride, tof, tof_stride, g, tp, values, v, vt, s))) return rc;
     return fold_views(image, v, scratch, vt, g, s);
 }

@@ -46,7 +46,7 @@ __device__ __forceinline__ void tie_path(const float *l, float tv, float yv, flo
     const float p = tie_project<G, TOF>(l, tv, lane, g, tp, x, xt);
     const float den = __fadd_rn(__fadd_rn(p, ad), eps);
     const float r = (rule == SRF_RATIO_DIV_NO_NAN) ? ((den == 0.0f) ? 0.0f : __fdiv_rn(yv, den)) : __fdiv_rn(yv, den);
-    if (want_ll && lane == 0 && den > 0.0f) ll += (double)yv * (double)__logf(den);
+    if (want_ll && lane == 0 && den > 0.0f) ll += (double)yv * log((double)den);  // FP64 term and sum
     tie_backproject<G, TOF>(l, tv, r, lane, g, tp, bp, bpt);
 }
 
@@ -176,7 +176,7 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
                 r = (den == 0.0f) ? 0.0f : __fdiv_rn(R.yv, den);
             else
                 r = __fdiv_rn(R.yv, den);
-            if (want_ll && lane == 0 && den > 0.0f) ll += (double)R.yv * (double)__logf(den);
+            if (want_ll && lane == 0 && den > 0.0f) ll += (double)R.yv * log((double)den);  // FP64 term and sum
         }
         if (r == 0.0f) continue;
         if (MODE == MODE_FUSED && single) {

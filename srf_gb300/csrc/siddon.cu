@@ -349,13 +349,6 @@ namespace srf {
 
 // TOF backprojection into caller-provided views (used by the no-allocation entry point in
 // noalloc.cu, which supplies its own y-fastest accumulator). Arguments are checked by the caller.
-int backprojection_tof_views(const float *lors, int64_t n, int stride, const float *tof,
-                             int tof_stride, const Grid &g, const TofParams &tp, const View &v,
-                             const View &vt, const float *values, cudaStream_t s) {
-    return launch_trace<true, RULES_BACK, SCATTER>(lors, n, stride, tof, tof_stride, g, tp, v, vt,
-                                                   values, nullptr, s);
-}
-
 // dst (x-fastest) += src (y-fastest) over a grid (used by noalloc.cu).
 int fold_views(float *dst, const View &d, const float *src, const View &sv, const Grid &g,
                cudaStream_t s) {

@@ -288,16 +288,29 @@ def correction_basis(device) -> torch.Tensor:
     return torch.stack(rows, 0).to(F32).contiguous()
 
 
+def _check_device_tensors(what: str, like: torch.Tensor, tensors) -> None:
+    """Raise ValueError unless every tensor is a contiguous CUDA tensor of its dtype on the device
+    of ``like`` (the kernels take raw pointers: a wrong one would reach the GPU unchecked)."""
+    for name, (t, dtype) in tensors.items():
+        if not t.is_cuda or t.device != like.device:
+            raise ValueError(f"{what}: {name} must be a CUDA tensor on {like.device}")
+        if not t.is_contiguous():
+            raise ValueError(f"{what}: {name} must be contiguous")
+        if t.dtype != dtype:
+            raise ValueError(f"{what}: {name} must be {dtype}, got {t.dtype}")
+
+
 def spot_fit(pred: torch.Tensor, bins: torch.Tensor, ref: torch.Tensor, basis: torch.Tensor,
              out: torch.Tensor, ridge: float = 1e-6) -> None:
     """srf_spot_fit: out[:k] = coefficients of the correction pred * (beta . basis) fitted to the
     even spot samples (bins, ref), out[k] / out[k + 1] = relative L2 difference of the corrected /
     uncorrected prediction on the odd samples. Asynchronous on the current stream."""
     k, nb = basis.shape
-    assert pred.dtype == F32 and ref.dtype == F32 and basis.dtype == F32 and bins.dtype == torch.int64
-    assert pred.numel() == nb and out.numel() >= k + 2 and bins.numel() == ref.numel()
-    assert all(t.is_cuda and t.is_contiguous() for t in (pred, bins, ref, basis, out)), \
-        "spot_fit takes contiguous CUDA tensors"
+    _check_device_tensors("spot_fit", pred, {"pred": (pred, F32), "bins": (bins, torch.int64),
+                                             "ref": (ref, F32), "basis": (basis, F32), "out": (out, F32)})
+    if pred.numel() != nb or out.numel() < k + 2 or bins.numel() != ref.numel():
+        raise ValueError("spot_fit: pred must have one entry per basis column, out at least k + 2 "
+                         "entries, and bins one entry per ref sample")
     call("srf_spot_fit", ptr(pred), i64(nb), ptr(bins), ptr(ref), i32(bins.numel()), ptr(basis), i32(k),
          f64(ridge), ptr(out), stream_ptr(pred.device))
 
@@ -305,9 +318,9 @@ def spot_fit(pred: torch.Tensor, bins: torch.Tensor, ref: torch.Tensor, basis: t
 def scale_by_basis(x: torch.Tensor, basis: torch.Tensor, beta: torch.Tensor) -> None:
     """srf_scale_by_basis: x *= beta . basis, in place (beta on the device)."""
     k, nb = basis.shape
-    assert x.dtype == F32 and x.numel() == nb and beta.numel() >= k
-    assert all(t.is_cuda and t.is_contiguous() for t in (x, basis, beta)), \
-        "scale_by_basis takes contiguous CUDA tensors"
+    _check_device_tensors("scale_by_basis", x, {"x": (x, F32), "basis": (basis, F32), "beta": (beta, F32)})
+    if x.numel() != nb or beta.numel() < k:
+        raise ValueError("scale_by_basis: x must have one entry per basis column and beta at least k")
     call("srf_scale_by_basis", ptr(x), i64(nb), ptr(basis), i32(k), ptr(beta), stream_ptr(x.device))
 
 

@@ -1,6 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the reference's own code.
 
-Run in a checkout that has the reference sources (``--reference``, default /root/reference):
+Run in a checkout that has the reference sources (``--reference``, default: the environment
+variable SRF_REFERENCE, else /root/reference):
 
 * siddon.npz -- the reference's Siddon device functions (srfnef/cc/siddon/siddon.cu.cc:12-656,
   srfnef/cc/siddon_tof/siddon_tof.cu.cc:14-707), compiled on the host by ``make -C oracle ref``
@@ -182,7 +183,7 @@ def make_host(out_path, reference):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("SRF_REFERENCE", "/root/reference"))
     a = ap.parse_args()
     make_siddon(os.path.join(HERE, "siddon.npz"))
     make_sss(os.path.join(HERE, "sss.npz"), a.reference)
