@@ -56,12 +56,14 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=20250101)
     ap.add_argument("--workload", default="clinical",
-                    choices=["clinical", "batched", "components", "surrogate", "profile", "autograd"],
+                    choices=["clinical", "batched", "components", "surrogate", "profile", "autograd",
+                             "mlem_small"],
                     help="clinical: the TOF OSEM headline; batched: 64 uneven studies; "
                          "components: every kernel of the path against the CPU oracle; "
                          "surrogate: learned scatter estimate against SSS (time, sinogram and "
                          "OSEM image agreement); profile: subset steps only, the case ncu captures; "
-                         "autograd: differentiable projector, 8 images, forward + backward")
+                         "autograd: differentiable projector, 8 images, forward + backward; "
+                         "mlem_small: non-TOF MLEM, 1e5 events, 640-crystal scanner, 64x64x16")
     ap.add_argument("--held-out", type=int, default=20, help="surrogate: held-out phantoms timed")
     ap.add_argument("--studies", type=int, default=64)
     ap.add_argument("--autotune", action="store_true", help="tune lanes/slabs per lane first")
@@ -181,8 +183,8 @@ def sum_over_ranks(v, ws, device=None):
 # ---------------------------------------------------------------- CPU (oracle) timing
 
 def cpu_sample_rate(lors_np, x_np, ic, tof, nsigma, threads):
-    """(pairs per second, pairs, seconds) of one fused subset pass (projection, ratio,
-    backprojection) of the oracle over lors_np."""
+    """(pairs per second, pairs, seconds, p, bp) of one fused subset pass (projection p, ratio,
+    backprojection bp) of the oracle over lors_np."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle as O
@@ -191,9 +193,32 @@ def cpu_sample_rate(lors_np, x_np, ic, tof, nsigma, threads):
     t0 = time.perf_counter()
     p, n1 = O.trace(lors_np, ic.shape, ic.center, ic.size, O.RULES_PROJ, O.GATHER, image=x_np, **kw)
     r = O.ratio(np.ones(len(p), np.float32), p, "full_tof")
-    _, n2 = O.trace(lors_np, ic.shape, ic.center, ic.size, O.RULES_BACK, O.SCATTER, values=r, **kw)
+    bp, n2 = O.trace(lors_np, ic.shape, ic.center, ic.size, O.RULES_BACK, O.SCATTER, values=r, **kw)
     dt = time.perf_counter() - t0
-    return (n1 + n2) / dt, n1 + n2, dt
+    return (n1 + n2) / dt, n1 + n2, dt, p, bp
+
+
+def subset_parity(st_x, samp_dev, x_np, p_ref, bp_ref, ic, tof, nsigma, dev):
+    """The GPU subset step on the oracle's sample and image: relative L2 of x * bp (the update
+    with a unit sensitivity) against the oracle's, and the FP64 sums y log(p + 1e-5) of both."""
+    import numpy as np
+    import torch
+    from srf_gb300 import kernels
+    from srf_gb300._lib import SRF_RATIO_DIV_NO_NAN
+    chk = kernels.SubsetState(ic.shape, ic.center, ic.size, dev, x0=st_x)
+    chk.subset(samp_dev, None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5, tof=tof, tof_nsigma=nsigma,
+               track_loglik=True)
+    chk.update(kernels.xfast(torch.ones(ic.shape, device=dev)), guard_zero=True)
+    got = chk.x.contiguous().cpu().numpy().astype(np.float64)
+    want = x_np.astype(np.float64) * bp_ref.astype(np.float64)
+    den = (p_ref + np.float32(1e-5)).astype(np.float64)
+    ll_ref = float(np.log(den[den > 0]).sum())
+    ll_gpu = float(chk.loglik.item())
+    return {"events": int(samp_dev.shape[0]),
+            "rel_l2_update": float(np.linalg.norm(got - want) / np.linalg.norm(want)),
+            "loglik_data_term_gpu": ll_gpu, "loglik_data_term_oracle": ll_ref,
+            "loglik_rel_diff": abs(ll_gpu - ll_ref) / max(abs(ll_ref), 1e-300),
+            "tolerance": 1e-5}
 
 
 def l2_peaks(dev):
@@ -248,7 +273,7 @@ def run_reference(a, ws, rank):
         cpu_sample_rate(lors[: max(1000, n // 20)], x, ic, tof, a.nsigma, threads)
     rates, secs = [], []
     for _ in range(a.steps):
-        r, pairs, dt = cpu_sample_rate(lors, x, ic, tof, a.nsigma, threads)
+        r, pairs, dt, _, _ = cpu_sample_rate(lors, x, ic, tof, a.nsigma, threads)
         rates.append(r)
         secs.append(dt)
     val = statistics.median(rates)
@@ -379,6 +404,103 @@ def run_batched(a, ws, rank, local):
             "gpu_launches": 2 * n_sub * max(a.steps, n_iter), "clocks": clk,
         }
         print(json.dumps(line), flush=True)
+
+
+def run_mlem_small(a, ws, rank, local):
+    """Non-TOF list-mode MLEM on the 640-crystal scanner (99 mm inner radius, 16 blocks of
+    10 x 4 crystals, 4 block rings): 1e5 seeded events of the water cylinder with six hot spheres
+    (snapped to crystal centres), image 64 x 64 x 16 at 2 mm, sensitivity image over all 409,600
+    ordered crystal pairs, 10 iterations of MlemFull's update (div_no_nan(y, p), x * bp / emap).
+
+    One step = one MLEM iteration with the inputs resident. The end-to-end leg is the whole job
+    through the drop-in, MlemFull(10, ...)() on numpy inputs: sensitivity image, 10 iterations,
+    image back as numpy. The CPU baseline is the oracle doing the same job on one thread; the
+    GPU job's image is compared with the oracle's."""
+    import numpy as np
+    import torch
+    import srf_gb300 as nef
+    from srf_gb300 import _lib, kernels, synth
+    from srf_gb300._lib import SRF_RATIO_DIV_NO_NAN
+    from srf_gb300.geometry import block_full_crystal_table
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.load()
+    sc, ic = synth.scanner_small(), synth.image_small()
+    n_ev, n_iter = 100_000, 10
+    act = synth.phantom_cylinder(ic, device=dev)
+    lors = synth.sample_events(sc, ic, act, n_ev, seed=a.seed + rank, tof_fwhm_ps=530.0, device=dev)
+    lors6 = lors[:, :6].contiguous()
+    stream = torch.cuda.current_stream(dev)
+    table = torch.as_tensor(block_full_crystal_table(sc), device=dev)
+    emap = kernels.emap_block_full(table, sc.nb_blocks_per_ring, ic.shape, ic.center, ic.size)
+    p_fwd = kernels.count_pairs(lors6, ic.shape, ic.center, ic.size, rules=0)
+    p_bwd = kernels.count_pairs(lors6, ic.shape, ic.center, ic.size, rules=1)
+    st = kernels.SubsetState(ic.shape, ic.center, ic.size, dev)
+
+    def iteration():
+        st.subset(lors6, None, rule=SRF_RATIO_DIV_NO_NAN, eps=0.0)
+        st.update(emap, guard_zero=True)
+
+    for _ in range(a.warmup):
+        iteration()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    barrier(ws)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        iteration()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms_step = max_over_ranks(e0.elapsed_time(e1) / a.steps, ws, dev)
+    upd = float(p_fwd + p_bwd)
+    # the whole job through the drop-in, numpy in and out
+    y_np = np.ones(n_ev, np.float32)
+    l_np = lors6.cpu().numpy()
+    lm = nef.Listmode(y_np, nef.Lors(l_np))
+    job = lambda: nef.MlemFull(n_iter, ic, sc, lm, None, None, None, None)()
+    job()
+    torch.cuda.synchronize()
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = job()
+    torch.cuda.synchronize()
+    job_s = (time.perf_counter() - t0) / reps
+    cpu = parity = None
+    if rank == 0 and not a.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        t0 = time.perf_counter()
+        em_ref = O.emap_block_full(block_full_crystal_table(sc), sc.nb_blocks_per_ring, ic.shape,
+                                   ic.center, ic.size)
+        ref = O.mlem(l_np, y_np, em_ref, ic.shape, ic.center, ic.size, n_iter, rule="full")
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": n_iter * upd / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"the whole job (sensitivity image + {n_iter} iterations) on the oracle, "
+                         f"{cpu_s:.2f} s", "job_s": cpu_s}
+        parity = {"rel_l2_image": O.rel_l2(out.data, ref),
+                  "rel_l2_emap": O.rel_l2(emap.contiguous().cpu().numpy(), em_ref), "tolerance": 1e-5}
+    if rank == 0:
+        print(json.dumps({
+            "metric": "non-TOF list-mode MLEM s/iter & LOR-voxel updates/s (640-crystal scanner)",
+            "value": upd / (ms_step / 1000.0), "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_step, "s_per_iter": ms_step / 1000.0,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded cylinder phantom, events snapped to crystals)",
+            "config": {"workload": "mlem_nontof_small", "events": n_ev, "image": ic.shape,
+                       "voxel_mm": 2.0, "crystals": int(sc.nb_crystals), "iterations": n_iter,
+                       "emap_lors": int(sc.nb_crystals) ** 2,
+                       "l2": "inputs L2-resident (2.4 MB of LORs), not flushed"},
+            "updates_per_iter": upd, "pairs_fwd": p_fwd, "pairs_bwd": p_bwd,
+            "job_s": job_s,
+            "e2e": {"value": n_iter * upd / job_s, "unit": UNIT, "h2d_bytes_per_step": int(l_np.nbytes + y_np.nbytes),
+                    "d2h_bytes_per_step": int(np.prod(ic.shape) * 4), "ms_per_step": 1000 * job_s,
+                    "path": "srf_gb300.MlemFull(10, ...)() on numpy inputs, sensitivity image included"},
+            "cpu_baseline": cpu, "parity": parity, "clocks": clk,
+            "gpu_launches": 2 * a.steps}), flush=True)
 
 
 def run_components(a, ws, rank, local):
@@ -712,58 +834,95 @@ def main():
     if a.workload == "autograd":
         run_autograd(a, ws, rank, local)
         return
+    if a.workload == "mlem_small":
+        run_mlem_small(a, ws, rank, local)
+        return
+    run_clinical(a, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_clinical(a, ws, rank, local):
+    """The headline: TOF list-mode OSEM on the clinical workload. With N ranks every subset's
+    events are split into N shards (strong scaling on the same events); each rank runs the fused
+    subset step on its shard and the ranks sum their backprojections with one all-reduce per
+    subset before the identical update."""
     import numpy as np
     import torch
-    from srf_gb300 import _lib, kernels, synth
+    from srf_gb300 import _lib, kernels
     from srf_gb300._lib import SRF_RATIO_DIV_NO_NAN
-    from srf_gb300.emap_generator import EmapGenerator
+    from srf_gb300.data import Emap, Listmode, Lors
+    from srf_gb300.distributed import ShardedOsem, subset_shards
     from srf_gb300.geometry import block_full_crystal_table
+    from srf_gb300.recon import OsemFullTof
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     _lib.load()
     _lib.set_group_lanes(a.lanes)
 
-    sc, ic, act, lors = make_workload(a, dev, rank)
+    sc, ic, act, lors = make_workload(a, dev, 0)  # every rank draws the same events
     tof = (sc.tof.tof_bin, sc.tof.tof_sigma2)
     n = lors.shape[0]
     n_sub = a.subsets
-    n_per = n // n_sub
+    stride_b = lors.stride(0) * 4
 
-    # sensitivity image over all crystal pairs (timed separately)
+    # sensitivity image over all crystal pairs (timed apart: first call, then warm best of 3)
     table = torch.as_tensor(block_full_crystal_table(sc), device=dev)
+    stream = torch.cuda.current_stream(dev)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     emap = kernels.emap_block_full(table, sc.nb_blocks_per_ring, ic.shape, ic.center, ic.size)
     torch.cuda.synchronize()
-    emap_s = time.perf_counter() - t0
-    em = (emap * (1.0 / n_sub)).permute(2, 1, 0).contiguous().permute(2, 1, 0)
+    emap_cold_s = time.perf_counter() - t0
+    emap_warm = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        emap = kernels.emap_block_full(table, sc.nb_blocks_per_ring, ic.shape, ic.center, ic.size)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        emap_warm.append(e0.elapsed_time(e1) / 1000.0)
+    del table
+    em = kernels.xfast(emap * (1.0 / n_sub))
 
-    # subset order: a seeded permutation, each subset contiguous
+    # the drop-in's inputs in host memory, in event order (rank 0 times the end-to-end leg)
+    host_lors = host_y = None
+    if not a.no_e2e:
+        host_lors = torch.empty(lors.shape, dtype=lors.dtype, pin_memory=True)
+        host_lors.copy_(lors)
+        host_y = torch.ones(n, dtype=torch.float32, pin_memory=True)
+
+    # subset order: a seeded permutation, each subset contiguous; this rank keeps its shards
     perm = torch.as_tensor(np.random.default_rng(a.seed).permutation(n), device=dev)
-    lors = lors.index_select(0, perm).contiguous()
+    lors = lors.index_select(0, perm)
     del perm
+    ranges = subset_shards(n, n_sub, rank, ws)
 
-    # exact LOR-voxel visits of one iteration
-    p_fwd = kernels.count_pairs(lors, ic.shape, ic.center, ic.size, rules=0, tof=tof, tof_nsigma=a.nsigma)
-    p_bwd = kernels.count_pairs(lors, ic.shape, ic.center, ic.size, rules=1, tof=tof, tof_nsigma=a.nsigma)
+    # exact LOR-voxel visits of one iteration (all ranks' events)
+    n_used = (n // n_sub) * n_sub
+    p_fwd = kernels.count_pairs(lors[:n_used], ic.shape, ic.center, ic.size, rules=0, tof=tof, tof_nsigma=a.nsigma)
+    p_bwd = kernels.count_pairs(lors[:n_used], ic.shape, ic.center, ic.size, rules=1, tof=tof, tof_nsigma=a.nsigma)
     updates_per_iter = p_fwd + p_bwd
+    shard_lors = [lors[lo:hi] for lo, hi in ranges]
+    mine = sum(hi - lo for lo, hi in ranges)
 
     st = kernels.SubsetState(ic.shape, ic.center, ic.size, dev)
-    stream = torch.cuda.current_stream(dev)
+    drv = ShardedOsem(st)
 
-    def iteration(lors_dev, ev=None):
+    def iteration(ev=None):
         for k in range(n_sub):
-            sl = lors_dev[k * n_per:(k + 1) * n_per]
             if ev is not None:
                 ev[k][0].record(stream)
-            st.subset(sl, None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5, tof=tof, tof_nsigma=a.nsigma)
+            st.subset(shard_lors[k], None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5, tof=tof, tof_nsigma=a.nsigma)
             if ev is not None:
                 ev[k][1].record(stream)
+            drv.reduce()
             st.update(em, guard_zero=True)
 
     for _ in range(a.warmup):
-        iteration(lors)
+        iteration()
     torch.cuda.synchronize()
 
     evs = [[[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
@@ -774,128 +933,128 @@ def main():
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     start.record(stream)
     for s_ in range(a.steps):
-        iteration(lors, evs[s_])
+        iteration(evs[s_])
     stop.record(stream)
     torch.cuda.synchronize()
     barrier(ws)
     clk = clocks.stop()
-    ms_total = start.elapsed_time(stop)
-    ms_total = max_over_ranks(ms_total, ws, dev)
+    ms_total = max_over_ranks(start.elapsed_time(stop), ws, dev)
     ms_step = ms_total / a.steps
     kern_ms = [evs[s_][k][0].elapsed_time(evs[s_][k][1]) for s_ in range(a.steps) for k in range(n_sub)]
     kern_ms_avg = sum(kern_ms) / len(kern_ms)
-    total_updates = sum_over_ranks(float(updates_per_iter), ws, dev)
-    value = total_updates / (ms_step / 1000.0)
+    value = float(updates_per_iter) / (ms_step / 1000.0)
 
-    # roofline of the dominant kernel (fused subset step): algorithmic bytes per launch
-    # = LOR rows read + 4 B per projector visit (image read) + 8 B per backprojector visit (RMW)
-    stride_b = lors.stride(0) * 4
-    alg_bytes = (n_per * stride_b + 4.0 * p_fwd / n_sub + 8.0 * p_bwd / n_sub)
-    achieved = alg_bytes / (kern_ms_avg / 1000.0) / 1e9
-    peak, peak_kind = peaks()
-
-    # L2 roofline of the same launch: gathers (4 B per projector visit) at the best-case L2 load
-    # rate plus reductions (one per backprojector visit) at the best-case L2 red rate
+    # roofline of the dominant kernel (the fused subset step) on this rank's launches. Its binding
+    # roof is L2: the gathers (4 B per projector visit) at the best-case L2 load rate plus the
+    # reductions (one red.add.f32 per backprojector visit) at the best-case L2 red rate, both
+    # measured in this run. Reductions count as load-equivalent bytes at the ratio of the two
+    # rates, so achieved / peak = (t_gather + t_red) / launch time.
+    share = mine / max(n_used, 1)
+    fwd_l = p_fwd * share / n_sub
+    bwd_l = p_bwd * share / n_sub
     l2 = l2_peaks(dev)
-    t_gather = 4.0 * p_fwd / n_sub / (l2["read_gbps"] * 1e9)
-    t_red = (p_bwd / n_sub) / l2["red_per_s"]
-    t_lor = n_per * stride_b / (peak * 1e9)
-    t_bound = max(t_lor, t_gather + t_red)
-    roofline_l2 = {"bound": "l2 gather + l2 red", "gather_bytes_per_launch": 4.0 * p_fwd / n_sub,
-                   "red_ops_per_launch": p_bwd / n_sub, "l2_read_peak_gbps": l2["read_gbps"],
-                   "l2_red_peak_per_s": l2["red_per_s"], "t_gather_ms": 1000 * t_gather,
-                   "t_red_ms": 1000 * t_red, "t_lor_stream_ms": 1000 * t_lor,
-                   "t_bound_ms": 1000 * t_bound, "launch_ms": kern_ms_avg,
-                   "frac": 1000 * t_bound / kern_ms_avg,
-                   "peaks": "measured in this run (srf_calib_l2, 32 MB buffer)"}
+    t_gather = 4.0 * fwd_l / (l2["read_gbps"] * 1e9)
+    t_red = bwd_l / l2["red_per_s"]
+    l2_bytes = 4.0 * fwd_l + bwd_l * (l2["read_gbps"] * 1e9 / l2["red_per_s"])
+    l2_achieved = l2_bytes / (kern_ms_avg / 1000.0) / 1e9
+    hbm_peak, hbm_kind = peaks()
+    lor_bytes = (mine / n_sub) * stride_b
+    roofline = {"bound": "l2", "achieved": l2_achieved, "peak": l2["read_gbps"], "unit": "GB/s",
+                "frac": l2_achieved / l2["read_gbps"],
+                "traffic": NCU_TRAFFIC_SUBSET if (mine // n_sub == 2_000_000 and a.nsigma == 3.0) else None,
+                "kernel": "k_osem_subset (fused projection+ratio+backprojection)",
+                "launch_ms": kern_ms_avg, "t_gather_ms": 1000 * t_gather, "t_red_ms": 1000 * t_red,
+                "gather_bytes_per_launch": 4.0 * fwd_l, "red_ops_per_launch": bwd_l,
+                "l2_red_peak_per_s": l2["red_per_s"],
+                "peak_kind": "measured in this run (srf_calib_l2: L2-resident 32 MB buffer)",
+                "achieved_def": "(gather bytes + red ops x read_peak/red_peak) / launch time"}
+    roofline_hbm = {"bound": "hbm", "achieved": lor_bytes / (kern_ms_avg / 1000.0) / 1e9,
+                    "peak": hbm_peak, "unit": "GB/s",
+                    "frac": lor_bytes / (kern_ms_avg / 1000.0) / 1e9 / hbm_peak,
+                    "alg_bytes_per_launch": lor_bytes, "peak_kind": hbm_kind,
+                    "alg_def": "the launch's LOR rows (28 B each); image and accumulators stay in L2"}
 
-    # end to end through the public API: every step copies its LORs from pinned host memory (per
-    # subset, on a copy stream, into one of two device buffers so that step s+1's copies overlap
-    # step s's kernels) and reads the image back
+    # FP64 Poisson log-likelihood of the final image over all events:
+    # sum_i log(p_i + 1e-5) - sum_j emap_j x_j (p from the projector, emap the full sensitivity)
+    llst = kernels.SubsetState(ic.shape, ic.center, ic.size, dev, x0=st.x)
+    for k in range(n_sub):
+        llst.subset(shard_lors[k], None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5, tof=tof,
+                    tof_nsigma=a.nsigma, track_loglik=True)
+    data_term = sum_over_ranks(float(llst.loglik.item()), ws, dev)
+    sens_term = float((emap.double() * st.x.double()).sum().item())
+    del llst
+
+    # end to end through the drop-in: OsemFullTof(1 iteration) on pinned host LORs and values --
+    # host-to-device copies, the device permutation, every subset step (with N ranks: this
+    # rank's shards and the per-subset all-reduce) -- and the image read back into pinned host
+    # memory, every step
     e2e = None
-    if not a.no_e2e:
-        host = torch.empty(lors.shape, dtype=lors.dtype, pin_memory=True)
-        host.copy_(lors)
-        torch.cuda.synchronize()
-        bufs = [torch.empty_like(lors), torch.empty_like(lors)]
-        free = [torch.cuda.Event(), torch.cuda.Event()]
-        for ev_ in free:
-            ev_.record(stream)
-        copy_stream = torch.cuda.Stream(dev)
-        out_host = torch.empty(ic.shape[::-1], dtype=torch.float32, pin_memory=True)
+    if host_lors is not None:
+        emap_img = Emap(emap, list(ic.center), list(ic.size))
+        rec = OsemFullTof(1, n_sub, ic, sc, Listmode(host_y, Lors(host_lors)), emap_img,
+                          tof_nsigma=a.nsigma, seed=a.seed, sharded=ws > 1)
+        out_host = torch.empty(ic.shape, dtype=torch.float32, pin_memory=True)
 
-        def e2e_step(s_):
-            buf = bufs[s_ % 2]
-            copy_stream.wait_event(free[s_ % 2])
-            ready = []
-            with torch.cuda.stream(copy_stream):
-                for k in range(n_sub):
-                    lo, hi = k * n_per, (n if k == n_sub - 1 else (k + 1) * n_per)
-                    buf[lo:hi].copy_(host[lo:hi], non_blocking=True)
-                    ev_ = torch.cuda.Event()
-                    ev_.record(copy_stream)
-                    ready.append(ev_)
-            for k in range(n_sub):
-                stream.wait_event(ready[k])
-                st.subset(buf[k * n_per:(k + 1) * n_per], None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5,
-                          tof=tof, tof_nsigma=a.nsigma)
-                st.update(em, guard_zero=True)
-            free[s_ % 2].record(stream)
-            out_host.copy_(st.x.permute(2, 1, 0), non_blocking=True)
+        def e2e_step():
+            img = rec()
+            out_host.copy_(img.data, non_blocking=True)
 
-        for s_ in range(2):
-            e2e_step(s_)
+        for _ in range(2):
+            e2e_step()
         torch.cuda.synchronize()
         barrier(ws)
         e_start, e_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e_start.record(stream)
-        copy_stream.wait_event(e_start)
         t0 = time.perf_counter()
-        for s_ in range(a.steps):
-            e2e_step(s_)
+        e_start.record(stream)
+        for _ in range(a.steps):
+            e2e_step()
         e_stop.record(stream)
         torch.cuda.synchronize()
         wall = (time.perf_counter() - t0) / a.steps
-        e_ms = max(e_start.elapsed_time(e_stop) / a.steps, 1000 * wall)
-        e_ms = max_over_ranks(e_ms, ws, dev)
-        e2e = {"value": total_updates / (e_ms / 1000.0), "unit": UNIT,
-               "h2d_bytes_per_step": int(host.numel() * 4), "d2h_bytes_per_step": int(out_host.numel() * 4),
-               "ms_per_step": e_ms, "copies": "per subset on a copy stream, double-buffered"}
-        del host, bufs
+        e_ms = max_over_ranks(max(e_start.elapsed_time(e_stop) / a.steps, 1000 * wall), ws, dev)
+        e2e = {"value": float(updates_per_iter) / (e_ms / 1000.0), "unit": UNIT,
+               "h2d_bytes_per_step": int(ws * (host_lors.numel() * 4 + host_y.numel() * 4)),
+               "d2h_bytes_per_step": int(ws * out_host.numel() * 4), "ms_per_step": e_ms,
+               "path": "srf_gb300.OsemFullTof(1 iteration, %d subsets)() per step on pinned host "
+                       "LORs; image copied back" % n_sub}
+        del rec
+    host_lors = host_y = None
 
-    cpu = None
+    # CPU baseline on a sample (the oracle, one thread); the GPU subset step on the same sample
+    # and image is checked against it
+    cpu = parity = None
     if rank == 0 and not a.no_cpu:
-        samp = lors[: a.cpu_sample].cpu().numpy()
+        samp = lors[: a.cpu_sample]
+        samp_np = samp.cpu().numpy()
         x_np = st.x.contiguous().cpu().numpy()
         threads = 1
-        rate, pairs, dt = cpu_sample_rate(samp, x_np, ic, tof, a.nsigma, threads)
+        rate, pairs, dt, p_ref, bp_ref = cpu_sample_rate(samp_np, x_np, ic, tof, a.nsigma, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{len(samp)} of {n} events: one TOF subset pass (projection, ratio, "
+               "sample": f"{len(samp_np)} of {n} events: one TOF subset pass (projection, ratio, "
                          f"backprojection) of the oracle, {pairs} visits in {dt:.2f} s"}
+        parity = subset_parity(st.x, samp, x_np, p_ref, bp_ref, ic, tof, a.nsigma, dev)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_step, "s_per_iter": ms_step / 1000.0,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "higher_is_better": True, "scaling": "strong" if ws > 1 else "weak",
+            "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded phantom, events snapped to crystals)",
-            "config": workload_config(a),
+            "config": dict(workload_config(a), parallelism=f"events sharded over {ws} rank(s), "
+                                                           "one all-reduce per subset"),
             "updates_per_iter": updates_per_iter, "pairs_fwd": p_fwd, "pairs_bwd": p_bwd,
-            "emap_s": emap_s, "emap_lors": int(sc.nb_crystals) ** 2,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak,
-                         "traffic": NCU_TRAFFIC_SUBSET if (n_per == 2_000_000 and a.nsigma == 3.0) else None,
-                         "kernel": "k_osem_subset (fused projection+ratio+backprojection)",
-                         "launch_ms": kern_ms_avg, "alg_bytes_per_launch": alg_bytes,
-                         "peak_kind": peak_kind},
-            "roofline_l2": roofline_l2,
+            "emap_s": min(emap_warm), "emap_s_first_call": emap_cold_s,
+            "emap_lors": int(sc.nb_crystals) ** 2,
+            "roofline": roofline, "roofline_hbm": roofline_hbm,
+            "parity": parity,
+            "loglik_fp64": {"value": data_term - sens_term, "data_term": data_term,
+                            "sensitivity_term": sens_term,
+                            "def": "sum_i log(p_i + 1e-5) - sum_j emap_j x_j after the timed iterations"},
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": a.steps * n_sub * 2,
         }
         print(json.dumps(line), flush=True)
-    if ws > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
 
 
 if __name__ == "__main__":

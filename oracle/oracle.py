@@ -35,6 +35,17 @@ GATHER, SCATTER = 0, 1
 _lib = None
 _ref = None
 
+# Host threads of the oracle traversals when a call does not say (1: the serial code path, whose
+# backprojection sums in the reference's LOR order). Large parity cases raise it.
+THREADS = 1
+
+
+def set_threads(n: int) -> int:
+    """Set the default thread count of the oracle traversals; returns the previous one."""
+    global THREADS
+    prev, THREADS = THREADS, max(1, int(n))
+    return prev
+
 _f32p = ctypes.POINTER(ctypes.c_float)
 _i32p = ctypes.POINTER(ctypes.c_int)
 
@@ -109,10 +120,12 @@ def _lor_args(lors: np.ndarray, tof: bool):
 
 
 def trace(lors, shape, center, size, rules, action, *, tof=False, tof_bin=0.0, tof_sigma2=0.0,
-          tof_nsigma=0.0, image=None, values=None, threads=1):
+          tof_nsigma=0.0, image=None, values=None, threads=None):
     """Generic traversal; returns (result, pairs). result is (N,) for GATHER, (nx,ny,nz) for SCATTER.
-    threads > 1 uses the OpenMP variant (backprojection summed in a different order)."""
+    threads > 1 uses the OpenMP variant (backprojection summed in a different order); None takes
+    the module default THREADS."""
     L = lib()
+    threads = THREADS if threads is None else threads
     fn = L.or_trace if threads <= 1 else (lambda *a: L.or_trace_mt(*a, threads))
     lors, stride, tof_ptr = _lor_args(lors, tof)
     n = lors.shape[0]

@@ -36,8 +36,11 @@ def device() -> torch.device:
 
 
 def to_dev(a, dtype=torch.float32) -> torch.Tensor:
+    """The array on the current CUDA device. A pinned host tensor is copied asynchronously in
+    stream order (the caller keeps it unchanged until the stream has passed the copy)."""
     if isinstance(a, torch.Tensor):
-        return a.to(device=device(), dtype=dtype)
+        pinned = a.device.type == "cpu" and a.is_pinned()
+        return a.to(device=device(), dtype=dtype, non_blocking=pinned)
     return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).to(device())
 
 

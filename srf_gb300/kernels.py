@@ -203,9 +203,18 @@ class SubsetState:
         else:
             self.x.copy_(x0)
         self.x_t = yfast(self.x)
-        self.bp = new_xfast(shape, device)
-        self.bp_t = new_yfast(shape, device)
+        # both backprojection accumulators in one flat buffer (one collective sums both)
+        nx, ny, nz = self.shape
+        v = nx * ny * nz
+        self._acc = torch.zeros(2 * v, dtype=F32, device=device)
+        self.bp = self._acc[:v].view(nz, ny, nx).permute(2, 1, 0)
+        self.bp_t = self._acc[v:].view(nz, nx, ny).permute(1, 2, 0)
         self.loglik = torch.zeros(1, dtype=torch.float64, device=device)
+
+    def accumulators(self) -> torch.Tensor:
+        """The flat buffer holding both backprojection accumulators (what an event-sharded
+        reconstruction sums over its ranks before the update)."""
+        return self._acc
 
     def subset(self, lors: torch.Tensor, y: Optional[torch.Tensor], *, rule: int, eps: float,
                tof: Optional[Tuple[float, float]] = None, tof_nsigma: float = 0.0,

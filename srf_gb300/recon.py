@@ -30,12 +30,28 @@ from typing import Any, Callable, Optional
 import numpy as np
 import torch
 
-from . import kernels
+from . import distributed, kernels
 from ._lib import SRF_RATIO_DIV_NO_NAN, SRF_RATIO_PLAIN
 from .data import Emap, Image, Listmode, _NefLike
 from .emap_generator import EmapGenerator
 from .functions import device, to_dev
 from .geometry import ImageConfig, PetEcatListmodeTrans, PetEcatScanner
+
+
+_PERMS: "dict" = {}
+
+
+def _device_permutation(seed: int, n: int, dev) -> torch.Tensor:
+    """numpy's default_rng(seed).permutation(n) on the device, kept for repeated calls with the
+    same seed and event count (the permutation depends on nothing else)."""
+    key = (int(seed), int(n), str(dev))
+    perm = _PERMS.get(key)
+    if perm is None:
+        if len(_PERMS) >= 4:
+            _PERMS.clear()
+        perm = torch.as_tensor(np.random.default_rng(seed).permutation(n), device=dev)
+        _PERMS[key] = perm
+    return perm
 
 
 def _emap_dev(emap) -> torch.Tensor:
@@ -128,7 +144,8 @@ class MlemFullTof(MlemFull):
         # mlem_full_tof.py:71-92: with a scatter correction, rerun on the corrected list mode
         if self.scatter_corr is None:
             return x
-        assert self.atten_corr is not None
+        if self.atten_corr is None:
+            raise ValueError("MlemFullTof: a scatter correction needs atten_corr (its u_map)")
         listmode_ = self.scatter_corr(x, self.atten_corr.u_map, self.scanner, self.listmode)
         return self._recon(listmode_)
 
@@ -195,17 +212,20 @@ class OsemFullTof(_NefLike):
     seed: int = 0
     snap: bool = False
     add: Any = None                      # per-event additive expected counts (e.g. scatter)
+    sharded: bool = False                # split each subset's events over the process group's ranks
+    group: Any = None                    # torch.distributed group (None: the default group)
 
     def prepare(self):
-        """Device-resident inputs: LORs and values permuted into subset order once."""
+        """Device-resident inputs: LORs and values permuted into subset order once (host tensors
+        in pinned memory are copied asynchronously; the permutation is applied on the device)."""
         lm = PetEcatListmodeTrans(self.scanner)(self.listmode) if self.snap else self.listmode
         dev = device()
         n = len(lm)
         lors = to_dev(lm.lors.data)
         y = to_dev(lm.data)
-        perm = torch.as_tensor(np.random.default_rng(self.seed).permutation(n), device=dev)
-        lors = lors.index_select(0, perm).contiguous()
-        y = y.index_select(0, perm).contiguous()
+        perm = _device_permutation(self.seed, n, dev)
+        lors = lors.index_select(0, perm)
+        y = y.index_select(0, perm)
         # a frozen record: the permuted additive term is cached beside the fields
         object.__setattr__(self, "_add", None if self.add is None
                            else to_dev(self.add).index_select(0, perm).contiguous())
@@ -216,18 +236,25 @@ class OsemFullTof(_NefLike):
     def run(self, lors: torch.Tensor, y: Optional[torch.Tensor], em: torch.Tensor,
             state: Optional[kernels.SubsetState] = None, n_iter: Optional[int] = None,
             track_loglik: bool = False) -> kernels.SubsetState:
+        """``n_iter`` passes over the subsets of the subset-ordered events. With ``sharded``, this
+        rank processes its contiguous share of every subset and the ranks' backprojections are
+        summed before each update (every rank ends with the same image)."""
         ic = self.image_config
         st = state or kernels.SubsetState(ic.shape, ic.center, ic.size, lors.device)
         n = lors.shape[0]
-        n_per = n // self.n_sub
+        rank, world = distributed.world_of(self.group) if self.sharded else (0, 1)
+        ranges = distributed.subset_shards(n, self.n_sub, rank, world)
+        driver = distributed.ShardedOsem(st, self.group) if self.sharded else None
         tof = (self.scanner.tof.tof_bin, self.scanner.tof.tof_sigma2)
         add = getattr(self, "_add", None)
         for _ in range(self.n_iter if n_iter is None else n_iter):
-            for k in range(self.n_sub):
-                sl = slice(k * n_per, (k + 1) * n_per)
+            for lo, hi in ranges:
+                sl = slice(lo, hi)
                 st.subset(lors[sl], None if y is None else y[sl], rule=SRF_RATIO_DIV_NO_NAN,
                           eps=1e-5, tof=tof, tof_nsigma=self.tof_nsigma, track_loglik=track_loglik,
                           add=None if add is None else add[sl])
+                if driver is not None:
+                    driver.reduce()
                 st.update(em, guard_zero=True)
         return st
 
