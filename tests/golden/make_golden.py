@@ -181,6 +181,267 @@ def make_host(out_path, reference):
                         scatter_position=scat, P1=P1, P2=P2)
 
 
+# ---------------------------------------------------------------- reference framework under stubs
+
+class _Tensor(np.ndarray):
+    """Eager TF tensor stand-in: a numpy array with .numpy(); Python and NumPy scalars take the
+    array's dtype, as TF converts them (float32 stays float32)."""
+
+    def numpy(self):
+        return np.asarray(self)
+
+    def _bin(self, other, op):
+        if np.isscalar(other):
+            other = np.asarray(other, dtype=self.dtype)
+        return op(np.asarray(self), np.asarray(other)).view(_Tensor)
+
+    __add__ = lambda s, o: s._bin(o, np.add)
+    __radd__ = lambda s, o: s._bin(o, lambda a, b: np.add(b, a))
+    __sub__ = lambda s, o: s._bin(o, np.subtract)
+    __mul__ = lambda s, o: s._bin(o, np.multiply)
+    __rmul__ = lambda s, o: s._bin(o, lambda a, b: np.multiply(b, a))
+    __truediv__ = lambda s, o: s._bin(o, np.divide)
+
+
+def _t(a):
+    return np.asarray(a).view(_Tensor)
+
+
+def _tf_stub(oracle):
+    """tensorflow with the reference's op libraries bound to the reference's own Siddon device
+    functions compiled for the host (oracle/_ref). The ops take what the srfnef wrappers pass:
+    transposed LORs (6 or 7 x N) and images (nz, ny, nx), grid/center/size as lists."""
+    tf = types.ModuleType("tensorflow")
+    tf.Variable = lambda x: _t(np.array(x))
+    tf.constant = lambda x: _t(np.array(x))
+    tf.transpose = lambda x: _t(np.ascontiguousarray(np.asarray(x).T))
+
+    def div_no_nan(a, b):
+        a, b = np.asarray(a, np.float32), np.asarray(b, np.float32)
+        out = np.zeros(np.broadcast(a, b).shape, np.float32)
+        nz = b != 0
+        out[nz] = a[nz] / b[nz]
+        return _t(out)
+
+    tf.div_no_nan = div_no_nan
+
+    def geo(grid, center, size):
+        return [int(v) for v in grid], [float(v) for v in center], [float(v) for v in size]
+
+    class Ops:
+        def projection(self, lors, image, grid, center, size):
+            g, c, s = geo(grid, center, size)
+            return _t(oracle.ref_projection(np.asarray(image).T, np.asarray(lors).T, g, c, s))
+
+        def backprojection(self, image, lors, lors_value, grid, center, size):
+            g, c, s = geo(grid, center, size)
+            bp, _ = oracle.ref_backprojection(np.asarray(lors_value), np.asarray(lors).T, g, c, s)
+            return _t(np.ascontiguousarray(bp.T))
+
+        def projection_tof(self, lors, image, grid, center, size, tof_values, tof_bin, tof_sigma2):
+            g, c, s = geo(grid, center, size)
+            return _t(oracle.ref_projection(np.asarray(image).T, np.asarray(lors).T, g, c, s, tof=True,
+                                            tof_bin=float(tof_bin), tof_sigma2=float(tof_sigma2)))
+
+        def backprojection_tof(self, image, lors, lors_value, grid, center, size, tof_values, tof_bin,
+                               tof_sigma2):
+            g, c, s = geo(grid, center, size)
+            bp, _ = oracle.ref_backprojection(np.asarray(lors_value), np.asarray(lors).T, g, c, s, tof=True,
+                                              tof_bin=float(tof_bin), tof_sigma2=float(tof_sigma2))
+            return _t(np.ascontiguousarray(bp.T))
+
+    tf.load_op_library = lambda path: Ops()
+    return tf
+
+
+def load_reference_framework(reference):
+    """The reference's own containers (nef_class, Image/Listmode/Lors/Emap, Block, PetEcatScanner
+    properties), geometry functions, projector wrappers and MLEM/OSEM loops, imported from the
+    reference tree under stub modules for what this container lacks (TensorFlow and its op
+    libraries, tqdm, IO and plotting mixins, corrections). Returns the srfnef namespace."""
+    import oracle
+    oracle.build(ref=True)
+    for name in [m for m in sys.modules if m == "srfnef" or m.startswith("srfnef.")]:
+        del sys.modules[name]
+    sys.modules["tensorflow"] = _tf_stub(oracle)
+    root = os.path.join(reference, "srfnef")
+
+    def pkg(name, path=None):
+        m = types.ModuleType(name)
+        m.__path__ = [path] if path else []
+        sys.modules[name] = m
+        return m
+
+    def stub(name, **attrs):
+        m = types.ModuleType(name)
+        m.__dict__.update(attrs)
+        sys.modules[name] = m
+        return m
+
+    top = pkg("srfnef", root)
+    top.__version__ = "reference"
+    pkg("srfnef.base", os.path.join(root, "base"))
+    bt = importlib.import_module("srfnef.base.basic_types")
+    bb = importlib.import_module("srfnef.base.base")
+    for k in ("Optional", "List", "Any", "Tuple", "isinstance_", "NoneType", "eq_"):
+        setattr(top, k, getattr(bt, k))
+    top.nef_class, top.NefBaseClass = bb.nef_class, bb.NefBaseClass
+    pkg("srfnef.ops", os.path.join(root, "ops"))
+    pkg("srfnef.ops.common", os.path.join(root, "ops", "common"))
+    pkg("srfnef.ops.geometry", os.path.join(root, "ops", "geometry"))
+    for m in ("property_mixins", "arithmetic_mixins", "magic_method_mixins"):
+        importlib.import_module("srfnef.ops.common." + m)
+    stub("srfnef.ops.common.imshow_mixin", ImshowMixin=type("ImshowMixin", (), {}))
+    stub("srfnef.io", LoadMixin=type("LoadMixin", (), {}), SaveMixin=type("SaveMixin", (), {}))
+    stub("srfnef.utils", tqdm=lambda it, *a, **k: it, declare_eager_execution=lambda: None)
+    stub("srfnef.config", TF_USER_OP_PATH="")
+    geo = pkg("srfnef.geometry", os.path.join(root, "geometry"))
+    for m, names in (("pet_scanner", ["PetScanner"]), ("block", ["Block"]), ("tof_config", ["TofConfig"]),
+                     ("image_config", ["ImageConfig"]), ("pet_ecat_scanner", ["PetEcatScanner"])):
+        mod = importlib.import_module("srfnef.geometry." + m)
+        for nm in names:
+            setattr(geo, nm, getattr(mod, nm))
+            setattr(top, nm, getattr(mod, nm))
+    geo.PetCylindricalScanner = type("PetCylindricalScanner", (), {})
+    data = pkg("srfnef.data", os.path.join(root, "data"))
+    for m, nm in (("lors", "Lors"), ("listmode", "Listmode"), ("image", "Image"), ("emap", "Emap")):
+        cls = getattr(importlib.import_module("srfnef.data." + m), nm)
+        setattr(data, nm, cls)
+        setattr(top, nm, cls)
+    top.Sinogram = type("Sinogram", (), {})
+    fn = pkg("srfnef.functions", os.path.join(root, "functions"))
+    pkg("srfnef.functions.geometry", os.path.join(root, "functions", "geometry"))
+    g = importlib.import_module("srfnef.functions.geometry.pet_ecat_scanner")
+    dtp = pkg("srfnef.functions.data_transform", os.path.join(root, "functions", "data_transform"))
+    pe = importlib.import_module("srfnef.functions.data_transform.pet_ecat")
+
+    class PetListmodeTrans:  # functions/data_transform/__init__.py:41-48, ECAT branch only
+        def __init__(self, scanner):
+            self.scanner = scanner
+
+        def __call__(self, listmode):
+            return pe.PetEcatListmodeTrans(self.scanner)(listmode)
+
+    dtp.PetListmodeTrans = PetListmodeTrans
+    for m, nm in (("project", "Project"), ("back_project", "BackProject"), ("project_tof", "ProjectTof"),
+                  ("back_project_tof", "BackProjectTof")):
+        setattr(fn, nm, getattr(importlib.import_module("srfnef.functions." + m), nm))
+    fn.EmapGenerator = None
+    corr = stub("srfnef.corrections", AttenuationCorrect=type("AttenuationCorrect", (), {}))
+    corr.__path__ = []
+    stub("srfnef.corrections.scattering", ScatterCorrect=type("ScatterCorrect", (), {}))
+    stub("srfnef.corrections.psf", PsfCorrect=type("PsfCorrect", (), {}))
+    for m, nm in (("mlem", "Mlem"), ("mlem_full", "MlemFull"), ("mlem_full_tof", "MlemFullTof"),
+                  ("osem_full", "OsemFull")):
+        setattr(fn, nm, getattr(importlib.import_module("srfnef.functions." + m), nm))
+    top.EcatCrystalPosToIndex = g.EcatCrystalPosToIndex
+    top.EcatIndexToCrystalPos = g.EcatIndexToCrystalPos
+    top.PetEcatListmodeTrans = pe.PetEcatListmodeTrans
+    top.functions = fn
+    return top
+
+
+def _ref_scanner(R, sc):
+    """The reference's PetEcatScanner with the fields of an srf_gb300 scanner."""
+    b = sc.blocks
+    return R.PetEcatScanner(sc.inner_radius, sc.outer_radius, sc.nb_rings, sc.nb_blocks_per_ring, sc.gap,
+                            R.Block(list(b.size), list(b.shape)),
+                            R.TofConfig(sc.tof.tof_bin, sc.tof.tof_sigma2))
+
+
+def make_geometry(out_path, R):
+    """Crystal index <-> position and list-mode snapping from the reference's own functions
+    (functions/geometry/pet_ecat_scanner.py:15-89, functions/data_transform/pet_ecat.py:43-60),
+    on the small and the clinical scanner, at crystal centres and at jittered positions."""
+    from srf_gb300 import synth
+    rng = np.random.default_rng(2024)
+    arrays = {}
+    for name, sc in (("small", synth.scanner_small()), ("clinical", synth.scanner_clinical())):
+        rs = _ref_scanner(R, sc)
+        n = sc.nb_crystals
+        ind = np.arange(n) if n <= 4096 else np.sort(rng.choice(n, 4096, replace=False))
+        pos = R.EcatIndexToCrystalPos(rs)(ind)
+        # jittered hits: within +-0.45 crystal of a centre transaxially and axially, and up to
+        # half the crystal depth radially
+        k = len(ind)
+        u = np.stack([rng.uniform(-0.5, 0.5, k) * (rs.outer_radius - rs.inner_radius),
+                      rng.uniform(-0.45, 0.45, k) * rs.blocks.unit_size[1],
+                      rng.uniform(-0.45, 0.45, k) * rs.blocks.unit_size[2]], 1)
+        iblock = (ind // rs.blocks.shape[1] // rs.blocks.shape[2]) % rs.nb_blocks_per_ring
+        th = iblock * rs.angle_per_block
+        jit = pos.astype(np.float64).copy()
+        jit[:, 0] += u[:, 0] * np.cos(th) - u[:, 1] * np.sin(th)
+        jit[:, 1] += u[:, 0] * np.sin(th) + u[:, 1] * np.cos(th)
+        jit[:, 2] += u[:, 2]
+        jit = jit.astype(np.float32)
+        ids = R.EcatCrystalPosToIndex(rs)(jit)
+        ids_c = R.EcatCrystalPosToIndex(rs)(pos)
+        m = k // 2
+        tof = rng.normal(0, 60, (m, 1)).astype(np.float32)
+        lors7 = np.hstack([jit[:m], jit[m:2 * m], tof]).astype(np.float32)
+        lm = R.Listmode(np.ones(m, np.float32), R.Lors(lors7))
+        snapped7 = R.PetEcatListmodeTrans(rs)(lm).lors.data
+        lm6 = R.Listmode(np.ones(m, np.float32), R.Lors(np.ascontiguousarray(lors7[:, :6])))
+        snapped6 = R.PetEcatListmodeTrans(rs)(lm6).lors.data
+        arrays.update({f"{name}_ind": ind, f"{name}_pos": pos, f"{name}_jit": jit, f"{name}_ids": ids,
+                       f"{name}_ids_centres": ids_c, f"{name}_lors7": lors7, f"{name}_snapped7": snapped7,
+                       f"{name}_snapped6": snapped6,
+                       f"{name}_props": np.array([rs.average_radius, rs.axial_length, rs.angle_per_block,
+                                                  rs.nb_crystals_per_block, rs.nb_crystals_per_ring,
+                                                  rs.nb_crystals], np.float64)})
+    np.savez_compressed(out_path, **arrays)
+
+
+def make_loops(out_path, R):
+    """Images of the reference's own update loops (functions/mlem.py:28-45, mlem_full.py:47-72,
+    mlem_full_tof.py:43-69, osem_full.py:49-87) with its projector wrappers, the TF op calls
+    served by the reference's compiled device functions, on a small seeded case."""
+    import oracle
+    from srf_gb300 import synth
+    from srf_gb300.geometry import ImageConfig
+    sc = synth.scanner_small()
+    rs = _ref_scanner(R, sc)
+    shape, center, size = [32, 32, 8], [0.0, 0.0, 0.0], [128.0, 128.0, 32.0]
+    ic = ImageConfig(shape, center, size)
+    lors = synth.sample_events(sc, ic, synth.phantom_cylinder(ic), 2000, seed=606, tof_fwhm_ps=530.0).numpy()
+    lors6 = np.ascontiguousarray(lors[:, :6])
+    rng = np.random.default_rng(607)
+    emap = (0.5 + rng.random(shape)).astype(np.float32)
+    emap[0, :, :] = 0.0  # exercises the zero guard
+    counts = rng.integers(1, 4, len(lors)).astype(np.float32)
+    ric = R.ImageConfig(shape, center, size)
+    em = R.Emap(emap, center, size)
+    F = R.functions
+    ones = np.ones(len(lors), np.float32)
+    out = {"lors": lors, "emap": emap, "counts": counts, "shape": np.asarray(shape, np.int32),
+           "center": np.asarray(center, np.float32), "size": np.asarray(size, np.float32)}
+    out["mlem_full_tof"] = F.MlemFullTof(3, ric, rs, R.Listmode(ones, R.Lors(lors)), None, None, None, em)().data
+    out["mlem_full"] = F.MlemFull(3, ric, rs, R.Listmode(ones, R.Lors(lors6)), None, None, None, em)().data
+    out["mlem"] = F.Mlem(3, em)(R.Listmode(counts, R.Lors(lors6))).data
+    # OsemFull shuffles with numpy's global generator: seed it, and record the permutation drawn
+    np.random.seed(608)
+    perm = np.arange(len(lors))
+    np.random.shuffle(perm)
+    np.random.seed(608)
+    em_pos = R.Emap((emap + np.float32(0.25)).astype(np.float32), center, size)  # no zero guard in OsemFull
+    out["osem_full"] = F.OsemFull(4, 2, ric, rs, R.Listmode(ones, R.Lors(lors6)), None, None, None, None,
+                                  em_pos, None)().data
+    out["osem_perm"] = perm
+    out["osem_emap"] = em_pos.data
+    # the projector wrappers themselves (transposes and all), on the first events
+    img = rng.random(shape).astype(np.float32)
+    out["wrap_image"] = img
+    out["wrap_proj"] = F.Project("tf-eager")(R.Image(img, center, size), R.Lors(lors6[:300])).data
+    out["wrap_proj_tof"] = F.ProjectTof("tf-eager", rs.tof)(R.Image(img, center, size), R.Lors(lors[:300])).data
+    vals = rng.random(300).astype(np.float32)
+    out["wrap_values"] = vals
+    out["wrap_bp"] = F.BackProject("tf-eager")(R.Listmode(vals, R.Lors(lors6[:300])),
+                                             R.Image(img, center, size)).data
+    out["wrap_bp_tof"] = F.BackProjectTof("tf-eager", rs.tof)(R.Listmode(vals, R.Lors(lors[:300])),
+                                                           R.Image(img, center, size)).data
+    np.savez_compressed(out_path, **{k: np.asarray(v) for k, v in out.items()})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("SRF_REFERENCE", "/root/reference"))
@@ -188,7 +449,10 @@ def main():
     make_siddon(os.path.join(HERE, "siddon.npz"))
     make_sss(os.path.join(HERE, "sss.npz"), a.reference)
     make_host(os.path.join(HERE, "host.npz"), a.reference)
-    for f in ("siddon.npz", "sss.npz", "host.npz"):
+    R = load_reference_framework(a.reference)
+    make_geometry(os.path.join(HERE, "geometry.npz"), R)
+    make_loops(os.path.join(HERE, "loops.npz"), R)
+    for f in ("siddon.npz", "sss.npz", "host.npz", "geometry.npz", "loops.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

@@ -90,6 +90,7 @@ def test_clinical_tof_projection_and_backprojection(cuda_lib, oracle, clinical, 
     kw = dict(tof=True, tof_bin=t[0], tof_sigma2=t[1], tof_nsigma=nsigma)
     ref = oracle.projection(img, lors, ic.shape, ic.center, ic.size, **kw)
     got = kernels.project(_dev(lors), _dev(img), ic.center, ic.size, tof=t, tof_nsigma=nsigma).cpu().numpy()
+    print(f"clinical TOF projection nsigma={nsigma}: rel L2 {rel_l2(got, ref):.3e}")
     assert rel_l2(got, ref) <= TOL
     assert np.array_equal(got == 0, ref == 0)
     vals = np.random.default_rng(407).random(len(lors)).astype(np.float32)
@@ -132,6 +133,7 @@ def test_clinical_osem_subset_step(cuda_lib, oracle, clinical, nsigma):
     r = oracle.ratio(np.ones(len(lors), np.float32), p, "full_tof")
     bp = oracle.backprojection(r, lors, ic.shape, ic.center, ic.size, **kw)
     want = (img * bp / oracle.guard_emap(emap)).astype(np.float32)
+    print(f"clinical subset step nsigma={nsigma}: rel L2 {rel_l2(got, want):.3e}")
     assert rel_l2(got, want) <= TOL
     den = (p + np.float32(1e-5)).astype(np.float64)
     terms = np.log(den[den > 0])
@@ -140,9 +142,18 @@ def test_clinical_osem_subset_step(cuda_lib, oracle, clinical, nsigma):
 
 
 def test_clinical_osem_tof_two_subsets(cuda_lib, oracle, clinical):
-    """One iteration of OsemFullTof with two subsets (3 sigma) against the oracle's loop."""
+    """One iteration of OsemFullTof with two subsets (3 sigma) from x = 1 against the oracle's
+    loop, on 2e6 events: a tenth of the benchmark's (at 1e5 events per subset most voxels of the
+    4.4e6 see a handful of LORs, and the ratio y / p of LORs through such voxels amplifies FP32
+    rounding beyond any fixed bound)."""
+    import torch
     import srf_gb300 as nef
-    sc, ic, lors, emap = clinical["scanner"], clinical["ic"], clinical["lors"], clinical["emap"]
+    from srf_gb300 import synth
+    sc, ic, emap = clinical["scanner"], clinical["ic"], clinical["emap"]
+    dev = torch.device("cuda", 0)
+    act = synth.phantom_body(ic, seed=404, device=dev)
+    lors = synth.sample_events(sc, ic, act, 10 * N_EVENTS, seed=410, tof_fwhm_ps=530.0,
+                               device=dev).cpu().numpy()
     lm = nef.Listmode(np.ones(len(lors), np.float32), nef.Lors(lors))
     em = nef.Emap(emap, ic.center, ic.size)
     out = nef.OsemFullTof(1, 2, ic, sc, lm, em, tof_nsigma=3.0, seed=409)()
@@ -150,7 +161,9 @@ def test_clinical_osem_tof_two_subsets(cuda_lib, oracle, clinical):
     ref = oracle.osem(lors, lm.data, emap, ic.shape, ic.center, ic.size, 2, 2, perm,
                       rule="full_tof", emap_scale=0.5, guard=True, subset_index="mod", tof=True,
                       tof_bin=sc.tof.tof_bin, tof_sigma2=sc.tof.tof_sigma2, tof_nsigma=3.0)
-    assert rel_l2(out.data, ref) <= TOL
+    err = rel_l2(out.data, ref)
+    print(f"clinical OSEM 2 subsets: rel L2 {err:.3e}")
+    assert err <= TOL
 
 
 def test_clinical_emap_block_columns(cuda_lib, oracle, clinical):
