@@ -260,6 +260,28 @@ int srf_attenuation(const float *lors, int64_t n, int32_t lor_stride, const floa
                     const int64_t umap_strides[3], const int32_t grid[3], const float center[3],
                     const float size[3], const float *values, float *out, void *stream);
 
+/* ------------------------------------------------------------------ image warping */
+/* Replace the TF ops Deform, Shift, ShiftZ, Rotate (srfnef/cc/deform/deform.cc:12-51, kernels
+ * deform.cu.cc:13-174) and their texture-library twins with DeformInvert (deform_tex.cc,
+ * deform_tex.cu.cc:15-420), called by srfnef/ops/deform_mixins.py:18-89. Images and
+ * displacement fields (in voxels) are x-fastest (index ix + iy*nx + iz*nx*ny), out is written
+ * in full. texture_rule != 0: the texture library's rules (clamped linear reads at position + 0.5,
+ * Shift/ShiftZ sampling at i - m), with FP32 interpolation weights; 0: the plain library's
+ * (voxels whose neighbourhood leaves the image are 0). Grid and parameters are passed by value;
+ * the reference copies the grid from the device on every call. */
+int srf_deform(const float *image, const float *mx, const float *my, const float *mz,
+               const int32_t grid[3], int32_t texture_rule, float *out, void *stream);
+int srf_shift(const float *image, float mx, float my, float mz, const int32_t grid[3],
+              int32_t texture_rule, float *out, void *stream);
+int srf_shift_z(const float *image, float mz, const int32_t grid[3], int32_t texture_rule,
+                float *out, void *stream);
+int srf_rotate(const float *image, float cos_phi, float sin_phi, const int32_t grid[3],
+               int32_t texture_rule, float *out, void *stream);
+/* The inverse displacement field (deform_tex.cu.cc:78-100): per voxel, `iterations` (0..1000;
+ * the reference uses 30) fixed-point steps x <- -mx(x + i), y <- -my(.), z <- -mz(.) from 0. */
+int srf_deform_invert(const float *mx, const float *my, const float *mz, const int32_t grid[3],
+                      int32_t iterations, float *out_mx, float *out_my, float *out_mz, void *stream);
+
 /* ------------------------------------------------------------------ sensitivity image */
 
 /* emap += sum over all ordered crystal pairs of the non-TOF backprojection of 1, generated on

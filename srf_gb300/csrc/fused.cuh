@@ -101,24 +101,25 @@ __device__ __forceinline__ bool proj_rule_at(float p1, float p2, bool xdom, bool
     return !((p2 > p1 && pp1 < p1) || (p2 < p1 && pp2 > p1));
 }
 
-// The rule keeps a contiguous slab range [pmlo, pmhi] (one side open): the bound is estimated in
-// double and then settled with the float predicate itself, so the range is exactly the rule's.
+// The rule keeps a contiguous slab range [pmlo, pmhi] (one side open): the bound is estimated
+// (within a slab) and then settled with the float predicate itself, so the range is exactly the
+// rule's. Single precision throughout: FP64 issues at a small fraction of the FP32 rate here.
 __device__ __forceinline__ void proj_slab_range(float p1, float p2, bool xdom, bool tof, float np2, int np,
                                                 int &pmlo, int &pmhi) {
     pmlo = -2;
     pmhi = np + 1;
-    const double a1 = (double)p1 + (double)np2, a2 = (double)p2 + (double)np2;
+    const float a1 = p1 + np2, a2 = p2 + np2;
     int upper = 0;  // +1: rule keeps ip <= bound; -1: keeps ip >= bound; 0: keeps every slab
-    double est = 0.0;
+    float est = 0.0f;
     if (!tof) {
-        if (p1 < p2) { upper = 1; est = floor(a2 - 1.0); } else { upper = -1; est = ceil(a2); }
+        if (p1 < p2) { upper = 1; est = floorf(a2 - 1.0f); } else { upper = -1; est = ceilf(a2); }
     } else if (p2 > p1) {
-        upper = -1; est = xdom ? floor(a1) + 1.0 : ceil(a1);
+        upper = -1; est = xdom ? floorf(a1) + 1.0f : ceilf(a1);
     } else if (p2 < p1) {
-        upper = 1; est = xdom ? ceil(a1 - 1.0) - 1.0 : floor(a1 - 1.0);
+        upper = 1; est = xdom ? ceilf(a1 - 1.0f) - 1.0f : floorf(a1 - 1.0f);
     }
     if (upper == 0) return;
-    int b = (int)fmin(fmax(est, -2.0), (double)np + 1.0);
+    int b = (int)fminf(fmaxf(est, -2.0f), (float)np + 1.0f);
     if (upper > 0) {
         for (int t = 0; t < 4 && b < np + 1 && proj_rule_at(p1, p2, xdom, tof, b + 1, np2); ++t) ++b;
         for (int t = 0; t < 4 && b > -2 && !proj_rule_at(p1, p2, xdom, tof, b, np2); ++t) --b;
@@ -177,7 +178,9 @@ __device__ __forceinline__ LorRec setup_rec(const float *l, float tv, float yv, 
                 R.kz / k.dz, -1.0f, (float)g.nz + 1.0f, np2, lo, hi);
     if (TOF) {
         const float tl = __fdiv_rn(__fdiv_rn(tv, k.dx_), L);
-        R.ratio1 = (float)((1.0 - (double)tl) * 0.5);
+        // the reference's (1.0 - tl) / 2 in double: 1 - tl is exact there and halving is exact,
+        // so its one rounding to float is RN(1 - tl) / 2, which FP32 computes bit for bit
+        R.ratio1 = __fmul_rn(__fsub_rn(1.0f, tl), 0.5f);
         if (k.nsig2 > 0.0f) {
             const float dpc = xdom ? 1.0f : k.dy;
             const float w = k.nsw / L;

@@ -9,6 +9,7 @@
 // accumulators in one pass over the image.
 #include "common.cuh"
 #include "fused.cuh"
+#include "lean.cuh"
 
 namespace srf {
 
@@ -80,10 +81,13 @@ __device__ __forceinline__ void chunk_candidates(const LorRun &run, const GridK 
 enum TraceMode : int { MODE_FUSED = 0, MODE_PROJ = 1, MODE_BACK = 2, MODE_ADJ = 3 };
 
 // LORs [base, base + 32) of one study: lane-parallel setup of the 32 records into wrecs, then
-// the warp's 32/G groups walk them (projection, ratio, backprojection per LOR). x/x_t and
-// bp/bp_t have equal strides (offsets are computed once for the gather and the scatter).
-template <int G, bool TOF, int U, int MODE = MODE_FUSED>
-__device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__restrict__ lors,
+// the warp's 32/G groups walk them (projection, ratio, backprojection per LOR) on the lean slab
+// loop (lean.cuh). x/x_t and bp/bp_t have equal strides (offsets are computed once for the
+// gather and the scatter). The projection walks the slabs the projector's endpoint rule keeps;
+// when that is the whole slab range and it fits one chunk of G*U slabs (the usual case with a
+// truncated TOF kernel), the backprojection reuses the chunk's offsets and weights.
+template <int G, bool TOF, int U, int MODE = MODE_FUSED, bool QDIV = false>
+__device__ __forceinline__ void osem_warp_batch(LeanRec *wrecs, const float *__restrict__ lors,
                                                 int64_t n, int stride, const float *__restrict__ tof,
                                                 int tof_stride, const Grid &g, const GridK &k,
                                                 const TofParams &tp, const float *__restrict__ y,
@@ -98,8 +102,8 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
     const bool have_t = xt.ptr != nullptr;
     {  // lane-parallel setup of the warp's next 32 LORs
         const int64_t i = base + lane32;
-        LorRec R = {};
-        R.lo = 1;
+        LeanRec E = {};
+        E.lo = 1;
         if (i < n) {
             const float *l = lors + i * stride;
             float lv[6];
@@ -107,87 +111,89 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
             for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
             const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
             const float yv = y ? __ldg(y + i) : 1.0f;
-            R = setup_rec<TOF>(lv, tv, yv, g, k);
+            LorRec R = setup_rec<TOF>(lv, tv, yv, g, k);
             R.ad = add ? __ldg(add + i) : 0.0f;
+            E = make_lean<TOF>(R, g, k, x.st, xt.st, have_t);
         }
-        store_rec(&wrecs[lane32], R);
+        store_lean(&wrecs[lane32], E);
     }
     __syncwarp();
     for (int j0 = 0; j0 < 32; j0 += GPW) {
         const int j = j0 + gi;
-        const LorRec R = load_rec(&wrecs[j]);
+        const LeanRec E = load_lean(&wrecs[j]);
         const int64_t i = base + j;
-        if (!TOF && (R.flags & F_TIE)) {  // ties exist only under the non-TOF projector rule
+        if (!TOF && (E.flags & F_TIE)) {  // ties exist only under the non-TOF projector rule
             float lv[6];
             const float *l = lors + i * stride;
 #pragma unroll
             for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
             const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
             if (MODE == MODE_FUSED) {
-                tie_path<G, TOF>(lv, tv, R.yv, R.ad, lane, g, tp, x, xt, bp, bpt, rule, eps, ll, want_ll);
+                tie_path<G, TOF>(lv, tv, E.yv, E.ad, lane, g, tp, x, xt, bp, bpt, rule, eps, ll, want_ll);
             } else if (MODE == MODE_PROJ) {
                 const float p = tie_project<G, TOF>(lv, tv, lane, g, tp, x, xt);
                 if (lane == 0) out[i] = p;
             } else {
-                tie_backproject<G, TOF>(lv, tv, R.yv, lane, g, tp, bp, bpt);
+                tie_backproject<G, TOF>(lv, tv, E.yv, lane, g, tp, bp, bpt);
             }
             continue;
         }
-        const bool valid = R.flags & F_VALID;
-        const LorRun run = make_run(R, g, k, x.st, xt.st, have_t);
-        const float *xim = (!run.xdom && have_t) ? xt.ptr : x.ptr;
-        float *bim = (!run.xdom && have_t) ? bpt.ptr : bp.ptr;
-        const bool proj_ok = R.flags & F_PROJ;
-        const bool single = (run.hi - run.lo + 1) <= G * U;
+        const bool valid = E.flags & F_VALID;
+        const bool xdom = E.flags & F_XDOM;
+        const LeanAxes ax = lean_axes(E, g, x.st, xt.st, have_t);
+        const float *xim = (!xdom && have_t) ? xt.ptr : x.ptr;
+        float *bim = (!xdom && have_t) ? bpt.ptr : bp.ptr;
+        // the projector's slabs: [plo, phi] (empty when the projector skips the LOR)
+        const int plo = (E.flags & F_PROJ) ? max(E.lo, E.pmlo) : 1;
+        const int phi = (E.flags & F_PROJ) ? min(E.hi, E.pmhi) : 0;
+        const bool shared = (plo == E.lo) && (phi == E.hi) && (E.hi - E.lo + 1 <= G * U);
         int32_t o[U][3];
         float w[U][3];
-        bool pm[U];
         float acc = 0.0f;
         if (MODE != MODE_BACK && valid) {
-            for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
-                chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
-                if (proj_ok) {
-                    float xv[U][3];
+            const float ppmax = (float)(phi - E.ic);
+            for (int c0 = plo; c0 <= phi; c0 += G * U) {
+                lean_chunk<TOF, U, G, QDIV>(E, ax, c0, phi, ppmax, lane, o, w);
+                float xv[U][3];
 #pragma unroll
-                    for (int u = 0; u < U; ++u)
+                for (int u = 0; u < U; ++u)
 #pragma unroll
-                        for (int c = 0; c < 3; ++c)
-                            xv[u][c] = (pm[u] && w[u][c] != 0.0f) ? __ldg(xim + o[u][c]) : 0.0f;
+                    for (int c = 0; c < 3; ++c) xv[u][c] = (w[u][c] != 0.0f) ? __ldg(xim + o[u][c]) : 0.0f;
 #pragma unroll
-                    for (int u = 0; u < U; ++u)
+                for (int u = 0; u < U; ++u)
 #pragma unroll
-                        for (int c = 0; c < 3; ++c) acc = fmaf(xv[u][c], w[u][c], acc);
-                }
+                    for (int c = 0; c < 3; ++c) acc = fmaf(xv[u][c], w[u][c], acc);
             }
         }
         float r;
         if (MODE == MODE_BACK) {
             if (!valid) continue;
-            r = R.yv;
+            r = E.yv;
         } else {
-            const float p = group_sum<G>(acc) * R.invL2;
+            const float p = group_sum<G>(acc) * E.invL2;
             if (MODE == MODE_PROJ) {
                 if (lane == 0 && i < n) out[i] = p;  // 0 for a skipped LOR, as the reference's memset
                 continue;
             }
             if (!valid) continue;
-            const float den = __fadd_rn(__fadd_rn(p, R.ad), eps);
+            const float den = __fadd_rn(__fadd_rn(p, E.ad), eps);
             if (rule == SRF_RATIO_DIV_NO_NAN)
-                r = (den == 0.0f) ? 0.0f : __fdiv_rn(R.yv, den);
+                r = (den == 0.0f) ? 0.0f : __fdiv_rn(E.yv, den);
             else
-                r = __fdiv_rn(R.yv, den);
-            if (want_ll && lane == 0 && den > 0.0f) ll += (double)R.yv * log((double)den);  // FP64 term and sum
+                r = __fdiv_rn(E.yv, den);
+            if (want_ll && lane == 0 && den > 0.0f) ll += (double)E.yv * log((double)den);  // FP64 term and sum
         }
         if (r == 0.0f) continue;
-        if (MODE == MODE_FUSED && single) {
+        if (MODE == MODE_FUSED && shared) {
 #pragma unroll
             for (int u = 0; u < U; ++u)
 #pragma unroll
                 for (int c = 0; c < 3; ++c)
                     if (w[u][c] != 0.0f) atomicAdd(bim + o[u][c], r * w[u][c]);
         } else {
-            for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
-                chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
+            const float ppmax = (float)(E.hi - E.ic);
+            for (int c0 = E.lo; c0 <= E.hi; c0 += G * U) {
+                lean_chunk<TOF, U, G, QDIV>(E, ax, c0, E.hi, ppmax, lane, o, w);
 #pragma unroll
                 for (int u = 0; u < U; ++u)
 #pragma unroll
@@ -206,13 +212,13 @@ __device__ __forceinline__ void osem_warp_batch(LorRec *wrecs, const float *__re
 // thread at 5 blocks per SM) that is 20 resident warps per SM instead of 16 with 256-thread blocks.
 constexpr int kOsemBlock = 128;
 
-template <int G, bool TOF, int U, int MINB>
+template <int G, bool TOF, int U, int MINB, bool QDIV>
 __global__ void __launch_bounds__(kOsemBlock, MINB)
 k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
               int tof_stride, Grid g, TofParams tp, const float *__restrict__ y,
               const float *__restrict__ add, int rule, float eps, View x, View xt, View bp, View bpt,
               double *__restrict__ loglik) {
-    __shared__ LorRec recs[kOsemBlock / 32][32];
+    __shared__ LeanRec recs[kOsemBlock / 32][32];
     const int wib = threadIdx.x >> 5;
     const int lane32 = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -221,7 +227,7 @@ k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float
     const bool want_ll = loglik != nullptr;
     double ll = 0.0;
     for (int64_t base = warp * 32; base < n; base += nwarps * 32) {
-        osem_warp_batch<G, TOF, U>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, y, add, rule, eps, x, xt, bp, bpt, base, want_ll, ll);
+        osem_warp_batch<G, TOF, U, MODE_FUSED, QDIV>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, y, add, rule, eps, x, xt, bp, bpt, base, want_ll, ll);
     }
     if (want_ll) {
 #pragma unroll
@@ -233,27 +239,34 @@ k_osem_subset(const float *__restrict__ lors, int64_t n, int stride, const float
 // The standalone projector (MODE_PROJ: out[i] for every LOR of x / x_t) and backprojector
 // (MODE_BACK: values[i] into the accumulators bp / bp_t) on the fused kernel's traversal, for
 // srf_projection(_tof) and srf_backprojection(_tof).
-template <int G, bool TOF, int U, int MINB, int MODE>
+template <int G, bool TOF, int U, int MINB, int MODE, bool QDIV>
 __global__ void __launch_bounds__(kOsemBlock, MINB)
 k_trace_fused(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
               int tof_stride, Grid g, TofParams tp, const float *__restrict__ values, float *__restrict__ out,
               View v, View vt) {
-    __shared__ LorRec recs[kOsemBlock / 32][32];
+    __shared__ LeanRec recs[kOsemBlock / 32][32];
     const int wib = threadIdx.x >> 5;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const GridK k = make_gridk<TOF>(g, tp);
     double ll = 0.0;
     for (int64_t base = warp * 32; base < n; base += nwarps * 32)
-        osem_warp_batch<G, TOF, U, MODE>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, values, nullptr,
+        osem_warp_batch<G, TOF, U, MODE, QDIV>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, values, nullptr,
                                          SRF_RATIO_PLAIN, 0.0f, v, vt, v, vt, base, false, ll, out);
+}
+
+// The x-dominant in-plane coordinate is divided by dy = (sy / ny) / (sx / nx) in the reference;
+// dy == 1 (square transaxial voxels) makes that division an identity the kernels compile out.
+inline bool grid_qdiv(const Grid &g) {
+    const float dx_ = g.sx / (float)g.nx;
+    return (g.sy / (float)g.ny) / dx_ != 1.0f;
 }
 
 template <int G, bool TOF, int MODE>
 static int launch_trace_fused_g(const float *lors, int64_t n, int stride, const float *tof, int tof_stride,
                                 const Grid &g, const TofParams &tp, const float *values, float *out,
                                 const View &v, const View &vt, cudaStream_t s) {
-    auto kern = k_trace_fused<G, TOF, 4, 5, MODE>;
+    auto kern = grid_qdiv(g) ? k_trace_fused<G, TOF, 4, 5, MODE, true> : k_trace_fused<G, TOF, 4, 5, MODE, false>;
     unsigned blocks = grid_for(kern, n, kOsemBlock, 0, kOsemBlock);
     kern<<<blocks, kOsemBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, values, out, v, vt);
     return check_cuda("fused trace kernel launch");
@@ -525,7 +538,7 @@ static int launch_osem_g(const float *lors, int64_t n, int stride, const float *
                          const Grid &g, const TofParams &tp, const float *y, const float *add, int rule, float eps,
                          const View &x, const View &xt, const View &bp, const View &bpt,
                          double *loglik, cudaStream_t s) {
-    auto kern = k_osem_subset<G, TOF, U, MINB>;
+    auto kern = grid_qdiv(g) ? k_osem_subset<G, TOF, U, MINB, true> : k_osem_subset<G, TOF, U, MINB, false>;
     unsigned blocks = grid_for(kern, n, kOsemBlock, 0, kOsemBlock);
     kern<<<blocks, kOsemBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, y, add, rule, eps, x, xt, bp, bpt, loglik);
     return check_cuda("osem subset kernel launch");
@@ -689,7 +702,7 @@ template <int G, bool TOF, int U, int MINB>
 __global__ void __launch_bounds__(kOsemBlock, MINB)
 k_osem_batch(const srf_study *__restrict__ studies, int n_studies, const int64_t *__restrict__ boff,
              int64_t total_batches, TofParams tp, int rule, float eps, double *__restrict__ loglik) {
-    __shared__ LorRec recs[kOsemBlock / 32][32];
+    __shared__ LeanRec recs[kOsemBlock / 32][32];
     __shared__ int64_t soff[kMaxStudiesSmem + 1];
     __shared__ WarpStudy wst[kOsemBlock / 32];
     const bool staged = n_studies <= kMaxStudiesSmem;
@@ -721,9 +734,14 @@ k_osem_batch(const srf_study *__restrict__ studies, int n_studies, const int64_t
             __syncwarp();
         }
         if (!w.ok) continue;
-        osem_warp_batch<G, TOF, U>(recs[wib], w.lors, w.n, w.stride, w.tof, w.tof_stride, w.g, w.k, tp,
-                                   w.y, nullptr, rule, eps, w.x, w.xt, w.bp, w.bpt,
-                                   (b - off[s]) * 32, want_ll, ll);
+        if (w.k.dy_one)  // uniform over the warp (one study)
+            osem_warp_batch<G, TOF, U, MODE_FUSED, false>(recs[wib], w.lors, w.n, w.stride, w.tof, w.tof_stride,
+                                                          w.g, w.k, tp, w.y, nullptr, rule, eps, w.x, w.xt,
+                                                          w.bp, w.bpt, (b - off[s]) * 32, want_ll, ll);
+        else
+            osem_warp_batch<G, TOF, U, MODE_FUSED, true>(recs[wib], w.lors, w.n, w.stride, w.tof, w.tof_stride,
+                                                         w.g, w.k, tp, w.y, nullptr, rule, eps, w.x, w.xt,
+                                                         w.bp, w.bpt, (b - off[s]) * 32, want_ll, ll);
     }
     if (want_ll) {
 #pragma unroll

@@ -279,11 +279,20 @@ def scanner_args(scanner):
     return d, s
 
 
-def snap(lors: torch.Tensor, scanner, want_ids: bool = False):
-    """Endpoints snapped to crystal centres (columns past 6 kept); optionally the crystal ids."""
+def snap(lors: torch.Tensor, scanner, want_ids: bool = False, out: Optional[torch.Tensor] = None):
+    """Endpoints snapped to crystal centres (columns 6 .. out's width - 1 kept); optionally the
+    crystal ids. ``out`` (N, >= 6) float32 rows with unit column stride, default like ``lors``."""
     _require_cuda(lors, "lors")
     n, stride = lors.shape[0], lors.stride(0)
-    out = torch.empty_like(lors)
+    if lors.dim() != 2 or lors.shape[1] < 6 or lors.stride(1) != 1:
+        raise ValueError("lors must be (N, >= 6) rows with unit column stride")
+    if out is None:
+        out = torch.empty_like(lors)
+    else:
+        _require_cuda(out, "out")
+        if out.dim() != 2 or out.shape[0] != n or out.shape[1] < 6 or out.stride(1) != 1 \
+                or out.stride(0) < out.shape[1] or out.device != lors.device:
+            raise ValueError("out must be (N, >= 6) rows with unit column stride on the LORs' device")
     ids = torch.empty((n, 2), dtype=torch.int64, device=lors.device) if want_ids else None
     d, s = scanner_args(scanner)
     call("srf_listmode_snap", ptr(lors), i64(n), i32(stride), d, s, ptr(out), i32(out.stride(0)),
