@@ -51,31 +51,6 @@ __device__ __forceinline__ void tie_path(const float *l, float tv, float yv, flo
     tie_backproject<G, TOF>(l, tv, r, lane, g, tp, bp, bpt);
 }
 
-// U slabs of one chunk per lane: fast candidates for all (independent, so they interleave), then
-// the rare exact recomputation of the slabs whose floors sat within the rounding margin.
-template <bool TOF, int U>
-__device__ __forceinline__ void chunk_candidates(const LorRun &run, const GridK &k, int c0, int lane,
-                                                 int G, int32_t (&o)[U][3], float (&w)[U][3],
-                                                 bool (&pm)[U]) {
-    bool bad[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const int ip = c0 + lane + G * u;
-        const bool act = ip <= run.hi;
-        if (c0 + G * u <= run.hi) {  // uniform over the group: skip slots past the range
-            candidates_fast<TOF>(run, k, act ? ip : run.hi, act, o[u], w[u], pm[u], bad[u]);
-        } else {
-            o[u][0] = o[u][1] = o[u][2] = 0;
-            w[u][0] = w[u][1] = w[u][2] = 0.0f;
-            pm[u] = false;
-            bad[u] = false;
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-        if (bad[u]) candidates_exact<TOF>(run, k, c0 + lane + G * u, o[u], w[u], pm[u]);
-}
-
 // What a traversal of osem_warp_batch does per LOR: the fused OSEM step, or one of its two halves
 // on its own (the projector into out[i], or the backprojector of the values passed as y).
 enum TraceMode : int { MODE_FUSED = 0, MODE_PROJ = 1, MODE_BACK = 2, MODE_ADJ = 3 };
@@ -314,8 +289,8 @@ __device__ __forceinline__ void emap_endpoints(const float *__restrict__ table, 
     lv[3] = __ldg(e2); lv[4] = __ldg(e2 + 1); lv[5] = __ldg(e2 + 2);
 }
 
-template <int G, int U>
-__device__ __forceinline__ void emap_warp(LorRec *wrecs, const float *__restrict__ table, int nb, int m, int64_t n,
+template <int G, int U, bool QDIV>
+__device__ __forceinline__ void emap_warp(LeanRec *wrecs, const float *__restrict__ table, int nb, int m, int64_t n,
                                           const Grid &g, const GridK &k, const TofParams &tp, const View &v,
                                           const View &vt, int64_t base) {
     constexpr int GPW = 32 / G;
@@ -325,34 +300,34 @@ __device__ __forceinline__ void emap_warp(LorRec *wrecs, const float *__restrict
     const bool have_t = vt.ptr != nullptr;
     {
         const int64_t i = base + lane32;
-        LorRec R = {};
-        R.lo = 1;
+        LeanRec E = {};
+        E.lo = 1;
         if (i < n) {
             float lv[6];
             emap_endpoints(table, nb, m, i, lv);
-            R = setup_rec<false>(lv, 0.0f, 1.0f, g, k);
+            E = make_lean<false>(setup_rec<false>(lv, 0.0f, 1.0f, g, k), g, k, v.st, vt.st, have_t);
         }
-        store_rec(&wrecs[lane32], R);
+        store_lean(&wrecs[lane32], E);
     }
     __syncwarp();
     for (int j0 = 0; j0 < 32; j0 += GPW) {
         const int j = j0 + gi;
-        const LorRec R = load_rec(&wrecs[j]);
+        const LeanRec E = load_lean(&wrecs[j]);
         const int64_t i = base + j;
-        if (R.flags & F_TIE) {  // the backprojector's own axis differs from the projector's: generic path
+        if (E.flags & F_TIE) {  // the backprojector's own axis differs from the projector's: generic path
             float lv[6];
             emap_endpoints(table, nb, m, i, lv);
             tie_backproject<G, false>(lv, 0.0f, 1.0f, lane, g, tp, v, vt);
             continue;
         }
-        if (!(R.flags & F_VALID)) continue;
-        const LorRun run = make_run(R, g, k, v.st, vt.st, have_t);
-        float *im = (!run.xdom && have_t) ? vt.ptr : v.ptr;
+        if (!(E.flags & F_VALID)) continue;
+        const LeanAxes ax = lean_axes(E, g, v.st, vt.st, have_t);
+        float *im = (!(E.flags & F_XDOM) && have_t) ? vt.ptr : v.ptr;
         int32_t o[U][3];
         float w[U][3];
-        bool pm[U];
-        for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
-            chunk_candidates<false, U>(run, k, c0, lane, G, o, w, pm);
+        const float ppmax = (float)(E.hi - E.ic);
+        for (int c0 = E.lo; c0 <= E.hi; c0 += G * U) {
+            lean_chunk<false, U, G, QDIV>(E, ax, c0, E.hi, ppmax, lane, o, w);
 #pragma unroll
             for (int u = 0; u < U; ++u)
 #pragma unroll
@@ -363,10 +338,10 @@ __device__ __forceinline__ void emap_warp(LorRec *wrecs, const float *__restrict
     __syncwarp();
 }
 
-template <int G, int U, int MINB>
+template <int G, int U, int MINB, bool QDIV>
 __global__ void __launch_bounds__(kOsemBlock, MINB)
 k_emap_fused(const float *__restrict__ table, int nb, int m, Grid g, View v, View vt) {
-    __shared__ LorRec recs[kOsemBlock / 32][32];
+    __shared__ LeanRec recs[kOsemBlock / 32][32];
     const int wib = threadIdx.x >> 5;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -374,13 +349,13 @@ k_emap_fused(const float *__restrict__ table, int nb, int m, Grid g, View v, Vie
     const GridK k = make_gridk<false>(g, tp);
     const int64_t n = (int64_t)nb * nb * (int64_t)m * m;
     for (int64_t base = warp * 32; base < n; base += nwarps * 32)
-        emap_warp<G, U>(recs[wib], table, nb, m, n, g, k, tp, v, vt, base);
+        emap_warp<G, U, QDIV>(recs[wib], table, nb, m, n, g, k, tp, v, vt, base);
 }
 
 int fused_emap(const float *table, int nb, int m, const Grid &g, const View &v, const View &vt, cudaStream_t s) {
     const int64_t n = (int64_t)nb * nb * (int64_t)m * m;
     if (n == 0) return ok();
-    auto kern = k_emap_fused<32, 4, 5>;
+    auto kern = grid_qdiv(g) ? k_emap_fused<32, 4, 5, true> : k_emap_fused<32, 4, 5, false>;
     unsigned blocks = grid_for(kern, n, kOsemBlock, 0, kOsemBlock);
     kern<<<blocks, kOsemBlock, 0, s>>>(table, nb, m, g, v, vt);
     return check_cuda("emap kernel launch");
@@ -411,8 +386,8 @@ __device__ __forceinline__ void tie_batch(const float *l, float tv, int lane, co
         });
 }
 
-template <int G, bool TOF, int U, int MODE>
-__device__ __forceinline__ void batch_warp(LorRec *wrecs, const float *__restrict__ lors, int64_t n, int stride,
+template <int G, bool TOF, int U, int MODE, bool QDIV>
+__device__ __forceinline__ void batch_warp(LeanRec *wrecs, const float *__restrict__ lors, int64_t n, int stride,
                                            const float *__restrict__ tof, int tof_stride, const Grid &g,
                                            const GridK &k, const TofParams &tp, int nb, int64_t bstride,
                                            const float *__restrict__ values, float *__restrict__ out,
@@ -424,22 +399,22 @@ __device__ __forceinline__ void batch_warp(LorRec *wrecs, const float *__restric
     const bool have_t = vt.ptr != nullptr;
     {
         const int64_t i = base + lane32;
-        LorRec R = {};
-        R.lo = 1;
+        LeanRec E = {};
+        E.lo = 1;
         if (i < n) {
             const float *l = lors + i * stride;
             float lv[6];
 #pragma unroll
             for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
             const float tv = TOF ? __ldg(tof + i * tof_stride) : 0.0f;
-            R = setup_rec<TOF>(lv, tv, 1.0f, g, k);
+            E = make_lean<TOF>(setup_rec<TOF>(lv, tv, 1.0f, g, k), g, k, v.st, vt.st, have_t);
         }
-        store_rec(&wrecs[lane32], R);
+        store_lean(&wrecs[lane32], E);
     }
     __syncwarp();
     for (int j0 = 0; j0 < 32; j0 += GPW) {
         const int j = j0 + gi;
-        const LorRec R = load_rec(&wrecs[j]);
+        const LeanRec E = load_lean(&wrecs[j]);
         const int64_t i = base + j;
         float acc[kMaxBatch], val[kMaxBatch];
         bool any = false;
@@ -449,28 +424,30 @@ __device__ __forceinline__ void batch_warp(LorRec *wrecs, const float *__restric
             val[b] = (MODE == MODE_ADJ && b < nb && i < n) ? __ldg(values + b * ostride + i) : 0.0f;
             any = any || val[b] != 0.0f;
         }
-        if (!TOF && (R.flags & F_TIE)) {  // ties exist only under the non-TOF projector rule
+        if (!TOF && (E.flags & F_TIE)) {  // ties exist only under the non-TOF projector rule
             float lv[6];
             const float *l = lors + i * stride;
 #pragma unroll
             for (int c = 0; c < 6; ++c) lv[c] = __ldg(l + c);
             if (MODE == MODE_PROJ || any) tie_batch<G, TOF, MODE>(lv, 0.0f, lane, g, tp, v, vt, nb, bstride, val, acc);
-        } else if ((R.flags & F_VALID) && (R.flags & F_PROJ) && (MODE == MODE_PROJ || any)) {
-            const LorRun run = make_run(R, g, k, v.st, vt.st, have_t);
-            float *im = (!run.xdom && have_t) ? vt.ptr : v.ptr;
+        } else if ((E.flags & F_VALID) && (E.flags & F_PROJ) && (MODE == MODE_PROJ || any)) {
+            const LeanAxes ax = lean_axes(E, g, v.st, vt.st, have_t);
+            float *im = (!(E.flags & F_XDOM) && have_t) ? vt.ptr : v.ptr;
             if (MODE == MODE_ADJ)
 #pragma unroll
-                for (int b = 0; b < kMaxBatch; ++b) val[b] *= R.invL2;
+                for (int b = 0; b < kMaxBatch; ++b) val[b] *= E.invL2;
+            // the projector's slabs: its endpoint rule keeps [pmlo, pmhi]
+            const int plo = max(E.lo, E.pmlo), phi = min(E.hi, E.pmhi);
+            const float ppmax = (float)(phi - E.ic);
             int32_t o[U][3];
             float w[U][3];
-            bool pm[U];
-            for (int c0 = run.lo; c0 <= run.hi; c0 += G * U) {
-                chunk_candidates<TOF, U>(run, k, c0, lane, G, o, w, pm);
+            for (int c0 = plo; c0 <= phi; c0 += G * U) {
+                lean_chunk<TOF, U, G, QDIV>(E, ax, c0, phi, ppmax, lane, o, w);
 #pragma unroll
                 for (int u = 0; u < U; ++u)
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        if (!(pm[u] && w[u][c] != 0.0f)) continue;
+                        if (w[u][c] == 0.0f) continue;
 #pragma unroll
                         for (int b = 0; b < kMaxBatch; ++b) {
                             if (b >= nb) continue;
@@ -480,7 +457,7 @@ __device__ __forceinline__ void batch_warp(LorRec *wrecs, const float *__restric
                     }
             }
 #pragma unroll
-            for (int b = 0; b < kMaxBatch; ++b) acc[b] *= R.invL2;
+            for (int b = 0; b < kMaxBatch; ++b) acc[b] *= E.invL2;
         }
         if (MODE == MODE_PROJ) {
 #pragma unroll
@@ -493,19 +470,19 @@ __device__ __forceinline__ void batch_warp(LorRec *wrecs, const float *__restric
     __syncwarp();
 }
 
-template <int G, bool TOF, int U, int MINB, int MODE>
+template <int G, bool TOF, int U, int MINB, int MODE, bool QDIV>
 __global__ void __launch_bounds__(kOsemBlock, MINB)
 k_trace_fused_batch(const float *__restrict__ lors, int64_t n, int stride, const float *__restrict__ tof,
                     int tof_stride, Grid g, TofParams tp, int nb, int64_t bstride,
                     const float *__restrict__ values, float *__restrict__ out, int64_t ostride, View v, View vt) {
-    __shared__ LorRec recs[kOsemBlock / 32][32];
+    __shared__ LeanRec recs[kOsemBlock / 32][32];
     const int wib = threadIdx.x >> 5;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const GridK k = make_gridk<TOF>(g, tp);
     for (int64_t base = warp * 32; base < n; base += nwarps * 32)
-        batch_warp<G, TOF, U, MODE>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, nb, bstride, values,
-                                    out, ostride, v, vt, base);
+        batch_warp<G, TOF, U, MODE, QDIV>(recs[wib], lors, n, stride, tof, tof_stride, g, k, tp, nb, bstride, values,
+                                          out, ostride, v, vt, base);
 }
 
 template <bool TOF, int MODE>
@@ -513,7 +490,7 @@ static int launch_fused_batch(const float *lors, int64_t n, int stride, const fl
                               const Grid &g, const TofParams &tp, int nb, int64_t bstride, const float *values,
                               float *out, int64_t ostride, const View &v, const View &vt, cudaStream_t s) {
     if (n == 0) return ok();
-    auto kern = k_trace_fused_batch<32, TOF, 4, 4, MODE>;
+    auto kern = grid_qdiv(g) ? k_trace_fused_batch<32, TOF, 4, 4, MODE, true> : k_trace_fused_batch<32, TOF, 4, 4, MODE, false>;
     unsigned blocks = grid_for(kern, n, kOsemBlock, 0, kOsemBlock);
     kern<<<blocks, kOsemBlock, 0, s>>>(lors, n, stride, tof, tof_stride, g, tp, nb, bstride, values, out, ostride, v, vt);
     return check_cuda("batched projector kernel launch");
