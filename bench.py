@@ -889,10 +889,23 @@ def run_clinical(a, ws, rank, local):
 
     # the drop-in's inputs in host memory, in event order (rank 0 times the end-to-end leg)
     host_lors = host_y = None
+    h2d_gbps = None
     if not a.no_e2e:
         host_lors = torch.empty(lors.shape, dtype=lors.dtype, pin_memory=True)
         host_lors.copy_(lors)
         host_y = torch.ones(n, dtype=torch.float32, pin_memory=True)
+        # raw host-to-device rate of one copy of the LOR array from pinned memory (what the
+        # end-to-end leg's copies cost)
+        scratch = torch.empty_like(lors)
+        scratch.copy_(host_lors, non_blocking=True)
+        torch.cuda.synchronize()
+        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        h0.record(stream)
+        scratch.copy_(host_lors, non_blocking=True)
+        h1.record(stream)
+        torch.cuda.synchronize()
+        h2d_gbps = host_lors.numel() * 4 / (h0.elapsed_time(h1) / 1000.0) / 1e9
+        del scratch
 
     # subset order: a seeded permutation, each subset contiguous; this rank keeps its shards
     perm = torch.as_tensor(np.random.default_rng(a.seed).permutation(n), device=dev)
@@ -1015,6 +1028,7 @@ def run_clinical(a, ws, rank, local):
         e2e = {"value": float(updates_per_iter) / (e_ms / 1000.0), "unit": UNIT,
                "h2d_bytes_per_step": int(ws * (host_lors.numel() * 4 + host_y.numel() * 4)),
                "d2h_bytes_per_step": int(ws * out_host.numel() * 4), "ms_per_step": e_ms,
+               "h2d_gbps_single_copy": h2d_gbps,
                "path": "srf_gb300.OsemFullTof(1 iteration, %d subsets)() per step on pinned host "
                        "LORs; image copied back" % n_sub}
         del rec
