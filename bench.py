@@ -38,7 +38,7 @@ UNIT = "LOR-voxel updates/s"
 FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes (read + write) of one k_osem_subset launch of this workload (2e6 TOF LORs, clinical
 # image), from ncu: profiles/k_osem_subset_tof_clinical_2M_lors.txt
-NCU_TRAFFIC_SUBSET = 127_165_696
+NCU_TRAFFIC_SUBSET = 124_260_096
 
 
 def parse():

@@ -711,14 +711,11 @@ k_osem_batch(const srf_study *__restrict__ studies, int n_studies, const int64_t
             __syncwarp();
         }
         if (!w.ok) continue;
-        if (w.k.dy_one)  // uniform over the warp (one study)
-            osem_warp_batch<G, TOF, U, MODE_FUSED, false>(recs[wib], w.lors, w.n, w.stride, w.tof, w.tof_stride,
-                                                          w.g, w.k, tp, w.y, nullptr, rule, eps, w.x, w.xt,
-                                                          w.bp, w.bpt, (b - off[s]) * 32, want_ll, ll);
-        else
-            osem_warp_batch<G, TOF, U, MODE_FUSED, true>(recs[wib], w.lors, w.n, w.stride, w.tof, w.tof_stride,
-                                                         w.g, w.k, tp, w.y, nullptr, rule, eps, w.x, w.xt,
-                                                         w.bp, w.bpt, (b - off[s]) * 32, want_ll, ll);
+        // one traversal for every study: the in-plane division (QDIV) is an identity for studies
+        // with square transaxial voxels (a second inlined copy for them would spill)
+        osem_warp_batch<G, TOF, U, MODE_FUSED, true>(recs[wib], w.lors, w.n, w.stride, w.tof, w.tof_stride,
+                                                     w.g, w.k, tp, w.y, nullptr, rule, eps, w.x, w.xt,
+                                                     w.bp, w.bpt, (b - off[s]) * 32, want_ll, ll);
     }
     if (want_ll) {
 #pragma unroll
