@@ -44,6 +44,29 @@ def to_dev(a, dtype=torch.float32) -> torch.Tensor:
     return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).to(device())
 
 
+_COPY_STREAMS: "dict" = {}
+
+
+def to_dev_overlapped(a, dtype=torch.float32) -> torch.Tensor:
+    """Like ``to_dev``, but a pinned host tensor travels on a side stream of its own: the current
+    stream waits for the copy only, so the copy overlaps device work already queued (a previous
+    reconstruction's kernels) instead of queueing behind it."""
+    if not (isinstance(a, torch.Tensor) and a.device.type == "cpu" and a.is_pinned()):
+        return to_dev(a, dtype)
+    dev = device()
+    side = _COPY_STREAMS.get(dev.index)
+    if side is None:
+        side = _COPY_STREAMS[dev.index] = torch.cuda.Stream(dev)
+    main = torch.cuda.current_stream(dev)
+    with torch.cuda.stream(side):
+        t = a.to(device=dev, dtype=dtype, non_blocking=True)
+    done = torch.cuda.Event()
+    done.record(side)
+    main.wait_event(done)
+    t.record_stream(main)  # the allocator keeps the block until main is past its uses
+    return t
+
+
 def like_input(t: torch.Tensor, ref, mode: str):
     """'tf-eager' returns the caller's array type; 'tf' keeps device tensors."""
     if mode == "tf-eager" and not isinstance(ref, torch.Tensor):

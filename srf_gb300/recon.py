@@ -34,7 +34,7 @@ from . import distributed, kernels
 from ._lib import SRF_RATIO_DIV_NO_NAN, SRF_RATIO_PLAIN
 from .data import Emap, Image, Listmode, _NefLike
 from .emap_generator import EmapGenerator
-from .functions import device, to_dev
+from .functions import device, to_dev, to_dev_overlapped
 from .geometry import ImageConfig, PetEcatListmodeTrans, PetEcatScanner
 
 
@@ -216,13 +216,15 @@ class OsemFullTof(_NefLike):
     group: Any = None                    # torch.distributed group (None: the default group)
 
     def prepare(self):
-        """Device-resident inputs: LORs and values permuted into subset order once (host tensors
-        in pinned memory are copied asynchronously; the permutation is applied on the device)."""
+        """Device-resident inputs: LORs and values permuted into subset order once. Host tensors
+        in pinned memory are copied on a side stream, overlapping the device work already queued
+        (with repeated calls, the previous reconstruction); the caller keeps them unchanged until
+        the call's result is read. The permutation is applied on the device."""
         lm = PetEcatListmodeTrans(self.scanner)(self.listmode) if self.snap else self.listmode
         dev = device()
         n = len(lm)
-        lors = to_dev(lm.lors.data)
-        y = to_dev(lm.data)
+        lors = to_dev_overlapped(lm.lors.data)
+        y = to_dev_overlapped(lm.data)
         perm = _device_permutation(self.seed, n, dev)
         lors = lors.index_select(0, perm)
         y = y.index_select(0, perm)

@@ -5,6 +5,8 @@ sensitivity on the device, and runs each OSEM subset step for *all* studies with
 ``srf_osem_subset_batch`` (a persistent kernel that walks every study's 32-LOR batches) and
 ``srf_osem_update_batch``. One full iteration (n_sub subsets) can be captured once into a CUDA
 graph and replayed, so an iteration over 64 studies costs 2 * n_sub kernel nodes and no host work.
+Alternatively (``capture(concurrent=True)``) the graph holds every study's own chain of subset and
+update kernels as independent branches over a pool of streams, which the GPU runs side by side.
 
 The per-study descriptors (``srf_study`` in include/srf_gb300.h) are built on the host from
 validated tensors and copied to the device once per subset.
@@ -114,17 +116,47 @@ class StudyBatch:
         for k in range(self.n_sub):
             self.subset(k)
 
-    def capture(self) -> None:
-        """Record one iteration into a CUDA graph (after one eager warm-up iteration)."""
+    def iteration_concurrent(self, n_streams: int = 8) -> None:
+        """One iteration as independent per-study chains (each study's subset and update kernels
+        in order) spread over ``n_streams`` streams forked from the current one and joined at the
+        end: the studies' kernels run side by side, each at the single-study kernel's efficiency,
+        and small studies fill the GPU together instead of one at a time."""
+        main = torch.cuda.current_stream(self.device)
+        streams = self._streams(n_streams)
+        for st_ in streams:
+            st_.wait_stream(main)
+        for j, st in enumerate(self.studies):
+            with torch.cuda.stream(streams[j % len(streams)]):
+                per = st.lors.shape[0] // self.n_sub
+                for k in range(self.n_sub):
+                    if per:
+                        st.state.subset(st.lors[k * per:(k + 1) * per],
+                                        None if st.y is None else st.y[k * per:(k + 1) * per],
+                                        rule=self.rule, eps=self.eps, tof=self.tof, tof_nsigma=self.tof_nsigma)
+                    st.state.update(st.emap, guard_zero=True)
+        for st_ in streams:
+            main.wait_stream(st_)
+
+    def _streams(self, n: int) -> List[torch.cuda.Stream]:
+        have = getattr(self, "_pool", [])
+        while len(have) < n:
+            have.append(torch.cuda.Stream(self.device))
+        self._pool = have
+        return have[:n]
+
+    def capture(self, concurrent: bool = False, n_streams: int = 8) -> None:
+        """Record one iteration into a CUDA graph (after one eager warm-up iteration): the two
+        batch kernels per subset, or with ``concurrent`` the per-study chains as parallel branches."""
+        run = (lambda: self.iteration_concurrent(n_streams)) if concurrent else self.iteration
         side = torch.cuda.Stream(self.device)
         side.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(side):
-            self.iteration()
+            run()
         torch.cuda.current_stream(self.device).wait_stream(side)
         torch.cuda.synchronize(self.device)
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
-            self.iteration()
+            run()
 
     def replay(self) -> None:
         if self.graph is None:

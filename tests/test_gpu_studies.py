@@ -83,6 +83,21 @@ def test_batch_matches_single_and_graph(studies_setup, oracle):
     torch.cuda.synchronize()
     for got, want in zip([x.cpu().numpy() for x in batch.images()], eager):
         assert rel_l2(got, want) <= TOL
+    # and as concurrent per-study chains: eager, then replayed from a graph with parallel branches
+    batch.reset()
+    for _ in range(2):
+        batch.iteration_concurrent(n_streams=3)
+    torch.cuda.synchronize()
+    for got, want in zip([x.cpu().numpy() for x in batch.images()], eager):
+        assert rel_l2(got, want) <= TOL
+    batch.reset()
+    batch.capture(concurrent=True, n_streams=3)
+    batch.reset()
+    for _ in range(2):
+        batch.replay()
+    torch.cuda.synchronize()
+    for got, want in zip([x.cpu().numpy() for x in batch.images()], eager):
+        assert rel_l2(got, want) <= TOL
 
 
 def test_autotune_picks_and_caches(studies_setup, tmp_path):
