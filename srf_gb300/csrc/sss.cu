@@ -29,14 +29,33 @@ namespace srf {
 constexpr int kAngles = 181;
 constexpr int kMaxScatterPoints = 12288;  // their mu values fill at most 48 KB of shared memory
 
-__device__ __forceinline__ double block_theta_d(int ncpr, int nbpr, int gb1, double px, double py, double pz) {
+// Block index of a crystal position (scatter_fraction.py:123-131, get_block_theta; its angle is
+// acos(x / |p|) with the 3-D norm, a quirk kept as is), in double.
+__device__ __forceinline__ int block_id_d(int ncpr, int nbpr, int gb1, double px, double py, double pz) {
     const double norm = sqrt(px * px + py * py + pz * pz);
     double th = acos(px / norm) / M_PI * 180.0;
     if (py < 0) th = 360.0 - th;
     double fixed = fmod(th + 180.0 / ncpr * gb1, 360.0);
     if (fixed < 0) fixed += 360.0;
-    const double id_block = floor(fixed / 360.0 * nbpr);
-    return id_block / nbpr * 2.0 * M_PI;
+    return (int)floor(fixed / 360.0 * nbpr);
+}
+
+// The same in FP32, re-evaluated in FP64 only when the block coordinate lies within 2e-3 of a
+// block boundary or |x / |p|| is within 1e-5 of 1 (where acos is ill-conditioned): crystals sit
+// inside their blocks, so the FP64 path stays cold. Every lane of a warp evaluates the same pair,
+// and FP64 issues at a small fraction of the FP32 rate on this part: in FP64 throughout this
+// step alone kept the FP64 pipe 84 % busy.
+__device__ __forceinline__ int block_id(int ncpr, int nbpr, int gb1, float px, float py, float pz) {
+    const float norm = sqrtf(px * px + py * py + pz * pz);
+    const float c = px / norm;
+    float th = acosf(c) * (float)(180.0 / M_PI);
+    if (py < 0) th = 360.0f - th;
+    float fixed = fmodf(th + 180.0f / ncpr * gb1, 360.0f);
+    if (fixed < 0) fixed += 360.0f;
+    const float q = fixed / 360.0f * nbpr;
+    const float fr = q - floorf(q);
+    if (fr < 2e-3f || fr > 1.0f - 2e-3f || fabsf(c) > 0.99999f) return block_id_d(ncpr, nbpr, gb1, px, py, pz);
+    return (int)floorf(q);
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -83,10 +102,10 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
         }
         const float ax = __ldg(cpos + 3 * a), ay = __ldg(cpos + 3 * a + 1), az = __ldg(cpos + 3 * a + 2);
         const float bx = __ldg(cpos + 3 * b), by = __ldg(cpos + 3 * b + 1), bz = __ldg(cpos + 3 * b + 2);
-        const double tha = block_theta_d(ncpr, nbpr, gb1, ax, ay, az);
-        const double thb = block_theta_d(ncpr, nbpr, gb1, bx, by, bz);
-        const float nax = (float)cos(tha), nay = (float)sin(tha);
-        const float nbx = (float)cos(thb), nby = (float)sin(thb);
+        // block normals at id / nbpr * 2 pi
+        float nax, nay, nbx, nby;
+        sincospif(2.0f * (float)block_id(ncpr, nbpr, gb1, ax, ay, az) / (float)nbpr, &nay, &nax);
+        sincospif(2.0f * (float)block_id(ncpr, nbpr, gb1, bx, by, bz) / (float)nbpr, &nby, &nbx);
         const float dabx = bx - ax, daby = by - ay, dabz = bz - az;
         const float ab2 = dabx * dabx + daby * daby + dabz * dabz;
         const float ab = sqrtf(ab2);
