@@ -14,9 +14,9 @@
 // formula expects cos theta; kn_formula.py:11).
 //
 // GB300 design: because theta is quantised to whole degrees, cos theta, 511/E', eff(E') and the
-// Klein-Nishina factor take at most 181 values; each block builds those tables in shared memory
-// (double precision, then rounded) and the inner loop is table lookups plus two power
-// functions; mu at each scatter point's nearest voxel is looked up once per block into shared
+// Klein-Nishina factor take at most 181 values; the host builds those tables once per call (double
+// precision, then rounded) and each block copies them into shared memory, so the inner loop is
+// table lookups plus two power functions; mu at each scatter point's nearest voxel is looked up once per block into shared
 // memory. One warp per LOR pair, lanes over scatter points, so the crystal-major emission and
 // attenuation rows are read coalesced. The angle is evaluated in FP32 with a bound on its
 // rounding error (from the law-of-cosines operands and acosf's accuracy) and re-evaluated in
@@ -58,11 +58,36 @@ __device__ __forceinline__ int block_id(int ncpr, int nbpr, int gb1, float px, f
     return (int)floorf(q);
 }
 
+// Per whole-degree angle: 511 / E' (the attenuation exponent), eff(E') and the Klein-Nishina factor
+// as the reference evaluates it (fkn receives the angle). Built on the host in double and rounded
+// to float, once per call, and passed by value (2.2 KB of kernel parameters).
+struct SssTables {
+    float g[kAngles], eff[kAngles], fk[kAngles];
+};
+
+static SssTables sss_tables(int low, int high, double res) {
+    SssTables T;
+    for (int t = 0; t < kAngles; ++t) {
+        const double ang = (double)t / 180.0 * M_PI;
+        const double c = std::cos(ang);
+        const double e_sc = 511.0 / (2.0 - c);
+        double eff = 0.0;
+        for (int e = low; e < high; e += 5) eff += std::exp(-((double)e - e_sc) * ((double)e - e_sc) / 2.0 / (res * res));
+        const double a = ang;  // the reference's fkn receives the angle
+        const double diff = 1.0 / ((2.0 - a) * (2.0 - a)) * ((1.0 + a * a) / 2.0 + (1.0 - a) * (1.0 - a) / 2.0 / (2.0 - a));
+        const double sigma = M_PI * (40.0 / 9.0 - 3.0 * std::log(3.0));
+        T.g[t] = (float)(511.0 / e_sc);
+        T.eff[t] = (float)eff;
+        T.fk[t] = (float)(diff / sigma);
+    }
+    return T;
+}
+
 __global__ void __launch_bounds__(kBlock)
 k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const float *__restrict__ cpos,
       const float *__restrict__ spos, int n_s, const float *__restrict__ em,
       const float *__restrict__ at, const float *__restrict__ umap, int u0, int u1, int u2,
-      float us0, float us1, float us2, int ncpr, int nbpr, int gb1, int low, int high, double res,
+      float us0, float us1, float us2, int ncpr, int nbpr, int gb1, const __grid_constant__ SssTables tab,
       float *__restrict__ scatter, float *__restrict__ scale) {
     __shared__ float t_g[kAngles], t_eff[kAngles], t_fk[kAngles];
     extern __shared__ float s_mu[];  // n_s entries: mu at the nearest voxel of each scatter point
@@ -78,17 +103,9 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
         s_mu[t] = mu;
     }
     for (int t = threadIdx.x; t < kAngles; t += blockDim.x) {
-        const double ang = (double)t / 180.0 * M_PI;
-        const double c = cos(ang);
-        const double e_sc = 511.0 / (2.0 - c);
-        double eff = 0.0;
-        for (int e = low; e < high; e += 5) eff += exp(-((double)e - e_sc) * ((double)e - e_sc) / 2.0 / (res * res));
-        const double a = ang;  // the reference's fkn receives the angle
-        const double diff = 1.0 / ((2.0 - a) * (2.0 - a)) * ((1.0 + a * a) / 2.0 + (1.0 - a) * (1.0 - a) / 2.0 / (2.0 - a));
-        const double sigma = M_PI * (40.0 / 9.0 - 3.0 * log(3.0));
-        t_g[t] = (float)(511.0 / e_sc);
-        t_eff[t] = (float)eff;
-        t_fk[t] = (float)(diff / sigma);
+        t_g[t] = tab.g[t];
+        t_eff[t] = tab.eff[t];
+        t_fk[t] = tab.fk[t];
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -153,10 +170,12 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
             const float a_a = __ldg(ata + s), a_b = __ldg(atb + s);
             const float Ia = a_a * exp2f(__log2f(a_b) * gexp) * __ldg(ema + s);
             const float Ib = exp2f(__log2f(a_a) * gexp) * a_b * __ldg(emb + s);
-            // area(S->A) uses A's block normal, area(S->B) B's
-            const float pa = (dax * nax + day * nay) / as;
-            const float pb = (dbx * nbx + dby * nby) / sb;
-            acc += pa * t_eff[ti] * pb * (t_fk[ti] * mu) * (Ia + Ib) / as2 / sb2;
+            // area(S->A) uses A's block normal, area(S->B) B's; the divisions by |SA|, |SB| and
+            // their squares as multiplications by correctly rounded reciprocals
+            const float ias = __frcp_rn(as), isb = __frcp_rn(sb);
+            const float pa = (dax * nax + day * nay) * ias;
+            const float pb = (dbx * nbx + dby * nby) * isb;
+            acc += pa * t_eff[ti] * pb * (t_fk[ti] * mu) * (Ia + Ib) * (ias * ias) * (isb * isb);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -201,7 +220,7 @@ extern "C" int srf_sss(const int32_t *pairs, int64_t n_pairs, const float *cryst
     k_sss<<<blocks, kBlock, smem, (cudaStream_t)stream>>>(
         pairs, n_pairs, n_crystals, crystal_pos, scatter_pos, n_scatter, sumup_emission, atten, umap,
         umap_shape[0], umap_shape[1], umap_shape[2], umap_size[0], umap_size[1], umap_size[2],
-        nb_crystals_per_ring, nb_blocks_per_ring, grid_block[1], low_energy, high_energy, res,
+        nb_crystals_per_ring, nb_blocks_per_ring, grid_block[1], sss_tables(low_energy, high_energy, res),
         scatter, scale);
     return check_cuda("sss kernel launch");
 }
