@@ -207,13 +207,14 @@ int srf_projection_adjoint(const float *lors, int64_t n, int32_t lor_stride, con
     Grid g; View v, vt; int rc;
     if ((rc = common_args(lors, n, lor_stride, image, image_strides, image_t, image_t_strides, grid, center, size, g, v, vt))) return rc;
     if (n > 0 && !values) return fail(SRF_EINVAL, "values must not be NULL");
+    // the batched adjoint traversal with one image (bstride 0)
     if (tof) {
         TofParams tp;
         if ((rc = check_tof(tof, n, tof_stride, tof_bin, tof_sigma2, tof_nsigma, tp))) return rc;
-        return launch_trace<true, RULES_PROJ, SCATTER>(lors, n, lor_stride, tof, tof_stride, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
+        return fused_adjoint_batch(lors, n, lor_stride, tof, tof_stride, g, tp, 1, 0, values, n, v, vt, (cudaStream_t)stream);
     }
     TofParams tp{0, 0, 0};
-    return launch_trace<false, RULES_PROJ, SCATTER>(lors, n, lor_stride, nullptr, 1, g, tp, v, vt, values, nullptr, (cudaStream_t)stream);
+    return fused_adjoint_batch(lors, n, lor_stride, nullptr, 1, g, tp, 1, 0, values, n, v, vt, (cudaStream_t)stream);
 }
 
 static int batch_args(int32_t n_images, int64_t batch_stride, int64_t row_stride, int64_t n,

@@ -63,6 +63,7 @@ __device__ __forceinline__ int block_id(int ncpr, int nbpr, int gb1, float px, f
 // to float, once per call, and passed by value (2.2 KB of kernel parameters).
 struct SssTables {
     float g[kAngles], eff[kAngles], fk[kAngles];
+    double cosd[kAngles];  // cos(t degrees): whole degrees of acos(x) = max{t : x <= cos(t deg)}
 };
 
 static SssTables sss_tables(int low, int high, double res) {
@@ -79,7 +80,9 @@ static SssTables sss_tables(int low, int high, double res) {
         T.g[t] = (float)(511.0 / e_sc);
         T.eff[t] = (float)eff;
         T.fk[t] = (float)(diff / sigma);
+        T.cosd[t] = c;
     }
+    T.cosd[kAngles - 1] = -1.0;
     return T;
 }
 
@@ -90,6 +93,7 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
       float us0, float us1, float us2, int ncpr, int nbpr, int gb1, const __grid_constant__ SssTables tab,
       float *__restrict__ scatter, float *__restrict__ scale) {
     __shared__ float t_g[kAngles], t_eff[kAngles], t_fk[kAngles];
+    __shared__ double t_cos[kAngles];
     extern __shared__ float s_mu[];  // n_s entries: mu at the nearest voxel of each scatter point
     for (int t = threadIdx.x; t < n_s; t += blockDim.x) {
         // kn_formula.py:12-14; outside the map counts as 0
@@ -106,6 +110,7 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
         t_g[t] = tab.g[t];
         t_eff[t] = tab.eff[t];
         t_fk[t] = tab.fk[t];
+        t_cos[t] = tab.cosd[t];
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -125,6 +130,8 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
         sincospif(2.0f * (float)block_id(ncpr, nbpr, gb1, bx, by, bz) / (float)nbpr, &nby, &nbx);
         const float dabx = bx - ax, daby = by - ay, dabz = bz - az;
         const float ab2 = dabx * dabx + daby * daby + dabz * dabz;
+        // |AB| in double, squared again as the reference does (kn_formula.py:36-41)
+        const double Dab = sqrt((double)dabx * dabx + (double)daby * daby + (double)dabz * dabz);
         const float ab = sqrtf(ab2);
         const float *ema = em + (int64_t)a * n_s, *emb = em + (int64_t)b * n_s;
         const float *ata = at + (int64_t)a * n_s, *atb = at + (int64_t)b * n_s;
@@ -153,14 +160,20 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
             }
             int ti;
             if (slow) {
+                // the cosine in double (as the reference) from the same float coordinates, then
+                // its whole degrees by comparison with cos(t deg): acos(x) >= t deg <=> x <= cos(t deg),
+                // starting from the FP32 estimate (no FP64 acos: FP64 issues at a small fraction
+                // of the FP32 rate here)
                 const double Dax = (double)ax - sx, Day = (double)ay - sy, Daz = (double)az - sz;
                 const double Dbx = (double)bx - sx, Dby = (double)by - sy, Dbz = (double)bz - sz;
-                const double Dab = sqrt((double)dabx * dabx + (double)daby * daby + (double)dabz * dabz);
                 const double Das = sqrt(Dax * Dax + Day * Day + Daz * Daz);
                 const double Dsb = sqrt(Dbx * Dbx + Dby * Dby + Dbz * Dbz);
                 double dargs = -(Das * Das + Dsb * Dsb - Dab * Dab) / (2 * Das * Dsb);
                 dargs = fmin(1.0, fmax(-1.0, dargs));
-                ti = (int)(acos(dargs) / M_PI * 180.0);
+                int t = min(max((int)(acosf((float)dargs) * (float)(180.0 / M_PI)), 0), kAngles - 1);
+                while (t < kAngles - 1 && dargs <= t_cos[t + 1]) ++t;
+                while (t > 0 && dargs > t_cos[t]) --t;
+                ti = t;
             } else {
                 ti = (int)deg;
             }
