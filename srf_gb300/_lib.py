@@ -5,6 +5,7 @@ no fallback: if the library is missing or fails to load, every entry point raise
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import os
 import threading
@@ -130,9 +131,26 @@ def yfast_strides(shape):
     return (ny, 1, nx * ny)
 
 
+_TUNING = {"lanes": 32, "slabs": 4}  # the library's defaults, mirrored by the setters below
+
+
 def set_group_lanes(lanes: int) -> None:
     call("srf_set_group_lanes", ctypes.c_int(lanes))
+    _TUNING["lanes"] = lanes
 
 
 def set_tuning(lanes: int, slabs_per_lane: int) -> None:
     call("srf_set_tuning", ctypes.c_int(lanes), ctypes.c_int(slabs_per_lane))
+    _TUNING.update(lanes=lanes, slabs=slabs_per_lane)
+
+
+@contextlib.contextmanager
+def tuning(lanes: int, slabs_per_lane: int):
+    """Launch variant for the calls inside the block (lanes per LOR, slabs per lane), restored
+    afterwards: e.g. 16 lanes for LORs that cross at most 64 slabs of a small grid."""
+    prev = (_TUNING["lanes"], _TUNING["slabs"])
+    set_tuning(lanes, slabs_per_lane)
+    try:
+        yield
+    finally:
+        set_tuning(*prev)

@@ -21,7 +21,8 @@
 // attenuation rows are read coalesced. The angle is evaluated in FP32 with a bound on its
 // rounding error (from the law-of-cosines operands and acosf's accuracy) and re-evaluated in
 // FP64 only when a whole degree lies within four times that bound, so its quantisation agrees
-// with a double-precision evaluation while the slow path stays rare.
+// with a double-precision evaluation while the slow path stays rare; those re-evaluations are
+// queued per warp and run 32 at a time.
 #include "common.cuh"
 
 namespace srf {
@@ -60,10 +61,15 @@ __device__ __forceinline__ int block_id(int ncpr, int nbpr, int gb1, float px, f
 
 // Per whole-degree angle: 511 / E' (the attenuation exponent), eff(E') and the Klein-Nishina factor
 // as the reference evaluates it (fkn receives the angle). Built on the host in double and rounded
-// to float, once per call, and passed by value (2.2 KB of kernel parameters).
+// to float, once per call, and passed by value (8.5 KB of kernel parameters). Whole degrees of
+// acos(x) are max{t : x <= cos(t deg)}; `start` gives, for each of kBuckets equal slices of
+// [-1, 1] in x, that t at the slice's upper end, from which a search over the cos table begins.
+constexpr int kBuckets = 4096;
 struct SssTables {
     float g[kAngles], eff[kAngles], fk[kAngles];
-    double cosd[kAngles];  // cos(t degrees): whole degrees of acos(x) = max{t : x <= cos(t deg)}
+    float cosf_[kAngles + 1];  // cos(t deg) rounded to float; [kAngles] = -2, below every cosine
+    double cosd[kAngles];      // cos(t deg) in double
+    unsigned char start[kBuckets];
 };
 
 static SssTables sss_tables(int low, int high, double res) {
@@ -83,17 +89,177 @@ static SssTables sss_tables(int low, int high, double res) {
         T.cosd[t] = c;
     }
     T.cosd[kAngles - 1] = -1.0;
+    for (int t = 0; t < kAngles; ++t) T.cosf_[t] = (float)T.cosd[t];
+    T.cosf_[kAngles] = -2.0f;
+    for (int b = 0; b < kBuckets; ++b) {
+        const double hi = std::min(1.0, -1.0 + 2.0 * (b + 1) / kBuckets);
+        int t = (int)std::floor(std::acos(hi) * 180.0 / M_PI);
+        T.start[b] = (unsigned char)std::min(std::max(t, 0), kAngles - 1);
+    }
     return T;
 }
 
-__global__ void __launch_bounds__(kBlock)
+// One crystal pair's geometry as every lane of its warp (or a lane of a deferred-angle flush) sees it.
+struct PairGeo {
+    float ax, ay, az, bx, by, bz;
+    float nax, nay, nbx, nby;  // block normals of A and B
+    float ab2;                 // |AB|^2 in FP32
+    int64_t ra, rb;            // offsets of A's and B's rows of the per-point tables
+};
+
+__device__ __forceinline__ PairGeo pair_geo(int a, int b, const float *__restrict__ cpos, int n_s, int ncpr, int nbpr, int gb1) {
+    PairGeo P;
+    P.ax = __ldg(cpos + 3 * a); P.ay = __ldg(cpos + 3 * a + 1); P.az = __ldg(cpos + 3 * a + 2);
+    P.bx = __ldg(cpos + 3 * b); P.by = __ldg(cpos + 3 * b + 1); P.bz = __ldg(cpos + 3 * b + 2);
+    // block normals at id / nbpr * 2 pi
+    sincospif(2.0f * (float)block_id(ncpr, nbpr, gb1, P.ax, P.ay, P.az) / (float)nbpr, &P.nay, &P.nax);
+    sincospif(2.0f * (float)block_id(ncpr, nbpr, gb1, P.bx, P.by, P.bz) / (float)nbpr, &P.nby, &P.nbx);
+    const float dabx = P.bx - P.ax, daby = P.by - P.ay, dabz = P.bz - P.az;
+    P.ab2 = dabx * dabx + daby * daby + dabz * dabz;
+    P.ra = (int64_t)a * n_s; P.rb = (int64_t)b * n_s;
+    return P;
+}
+
+// Scatter point s of pair P: the law-of-cosines operands in FP32.
+struct PointGeo {
+    float dax, day, dbx, dby;  // in-plane components of A - S and B - S (the area terms)
+    float as2, sb2, ias, isb;  // |SA|^2, |SB|^2 and their reciprocal square roots
+    float sx, sy, sz;
+};
+
+__device__ __forceinline__ PointGeo point_geo(const PairGeo &P, const float *__restrict__ spos, int s) {
+    PointGeo Q;
+    Q.sx = __ldg(spos + 3 * s); Q.sy = __ldg(spos + 3 * s + 1); Q.sz = __ldg(spos + 3 * s + 2);
+    Q.dax = P.ax - Q.sx; Q.day = P.ay - Q.sy;
+    const float daz = P.az - Q.sz;
+    Q.dbx = P.bx - Q.sx; Q.dby = P.by - Q.sy;
+    const float dbz = P.bz - Q.sz;
+    Q.as2 = Q.dax * Q.dax + Q.day * Q.day + daz * daz;
+    Q.sb2 = Q.dbx * Q.dbx + Q.dby * Q.dby + dbz * dbz;
+    Q.ias = rsqrtf(Q.as2); Q.isb = rsqrtf(Q.sb2);
+    return Q;
+}
+
+// Whole degrees of the scattering angle from the FP32 cosine, or -1 when the FP32 value cannot
+// decide them. With u = 2^-24: |SA|^2, |SB|^2 and |AB|^2 carry at most 5u relative error each
+// (the float differences and three roundings), the numerator N = |SA|^2 + |SB|^2 - |AB|^2 at most
+// 7u S (S = |SA|^2 + |SB|^2 + |AB|^2); rsqrtf is within 2 ulp, so 1 / den = rsqrt(|SA|^2) *
+// rsqrt(|SB|^2) / 2 is within 14u, and arg = -N / den is within 15u |arg| + 7u S / den <=
+// 22u S / den (S / den >= 1) of the cosine the double path computes. The angle is decided when
+// arg lies more than four times that bound (plus the 3e-8 rounding of the float cosine table)
+// from both cosines bracketing it; otherwise, and at |arg| = 1, the point goes to the double path.
+__device__ __forceinline__ int fast_angle(const PairGeo &P, const PointGeo &Q, const float *t_cf,
+                                          const unsigned char *t_start) {
+    const float S = Q.as2 + Q.sb2 + P.ab2;
+    const float iden = 0.5f * Q.ias * Q.isb;
+    float arg = -(Q.as2 + Q.sb2 - P.ab2) * iden;
+    arg = fminf(1.0f, fmaxf(-1.0f, arg));
+    const float Em = 4.0f * 1.32e-6f * S * iden + 4.0e-8f;
+    const int b = min(max((int)((arg + 1.0f) * (0.5f * kBuckets)), 0), kBuckets - 1);
+    int t = t_start[b];
+    while (t < kAngles - 1 && arg <= t_cf[t + 1]) ++t;
+    while (t > 0 && arg > t_cf[t]) --t;
+    if (t_cf[t] - arg <= Em || arg - t_cf[t + 1] <= Em) return -1;
+    return t;
+}
+
+// The cosine in double (as the reference) from the same float coordinates, then its whole
+// degrees by comparison with cos(t deg): acos(x) >= t deg <=> x <= cos(t deg), starting from the
+// FP32 estimate (no FP64 acos: FP64 issues at a small fraction of the FP32 rate here).
+__device__ __forceinline__ int slow_angle(const PairGeo &P, const PointGeo &Q, const double *t_cos) {
+    // |AB| in double from the float difference, squared again as kn_formula.py:36-41 does
+    const float dabx = P.bx - P.ax, daby = P.by - P.ay, dabz = P.bz - P.az;
+    const double Dab = sqrt((double)dabx * dabx + (double)daby * daby + (double)dabz * dabz);
+    const double Dax = (double)P.ax - Q.sx, Day = (double)P.ay - Q.sy, Daz = (double)P.az - Q.sz;
+    const double Dbx = (double)P.bx - Q.sx, Dby = (double)P.by - Q.sy, Dbz = (double)P.bz - Q.sz;
+    const double Das = sqrt(Dax * Dax + Day * Day + Daz * Daz);
+    const double Dsb = sqrt(Dbx * Dbx + Dby * Dby + Dbz * Dbz);
+    double dargs = -(Das * Das + Dsb * Dsb - Dab * Dab) / (2 * Das * Dsb);
+    dargs = fmin(1.0, fmax(-1.0, dargs));
+    int t = min(max((int)(acosf((float)dargs) * (float)(180.0 / M_PI)), 0), kAngles - 1);
+    while (t < kAngles - 1 && dargs <= t_cos[t + 1]) ++t;
+    while (t > 0 && dargs > t_cos[t]) --t;
+    return t;
+}
+
+// The term of scatter point s at whole-degree angle ti (FP32).
+__device__ __forceinline__ float point_term(const PairGeo &P, const PointGeo &Q, int s, int ti,
+                                            const float *__restrict__ em, const float *__restrict__ at,
+                                            const float *s_mu, const float *t_g, const float *t_eff,
+                                            const float *t_fk) {
+    const float gexp = t_g[ti];
+    const float a_a = __ldg(at + P.ra + s), a_b = __ldg(at + P.rb + s);
+    const float Ia = a_a * exp2f(__log2f(a_b) * gexp) * __ldg(em + P.ra + s);
+    const float Ib = exp2f(__log2f(a_a) * gexp) * a_b * __ldg(em + P.rb + s);
+    // area(S->A) uses A's block normal, area(S->B) B's; the divisions by |SA|, |SB| and their
+    // squares as multiplications by the reciprocal square roots of |SA|^2, |SB|^2
+    const float ias = Q.ias, isb = Q.isb;
+    const float pa = (Q.dax * P.nax + Q.day * P.nay) * ias;
+    const float pb = (Q.dbx * P.nbx + Q.dby * P.nby) * isb;
+    return pa * t_eff[ti] * pb * (t_fk[ti] * s_mu[s]) * (Ia + Ib) * (ias * ias) * (isb * isb);
+}
+
+// Deferred double-precision angles: a warp queues the (pair, point) items whose FP32 angle is
+// undecided (about 2e-3 of them) and evaluates them 32 at a time, one per lane, instead of
+// running the FP64 path for one or two lanes of a warp at a time. Entries pack pair << 14 | point.
+constexpr int kQueue = 64;
+constexpr int kPointBits = 14;
+static_assert(kMaxScatterPoints <= (1 << kPointBits), "point index field too narrow");
+
+// Evaluates the first `cnt` (<= 32) queued items of this warp, sums them per pair in queue order
+// (a run of one pair is summed by the run's first lane) and drops them from the queue. Sums of
+// pairs already written are added to their scatter values; the sum of pair `kcur`, the pair the
+// warp is still accumulating, is returned (to every lane). Every pair in the queue belongs to
+// this warp.
+__device__ __forceinline__ float flush_deferred(unsigned long long *q, float *qv, int &qn, int cnt, int64_t kcur, int lane,
+                                               const int32_t *__restrict__ pairs, const float *__restrict__ cpos,
+                                               const float *__restrict__ spos, int n_s,
+                                               const float *__restrict__ em, const float *__restrict__ at,
+                                               int ncpr, int nbpr, int gb1, const float *s_mu,
+                                               const float *t_g, const float *t_eff, const float *t_fk,
+                                               const double *t_cos, float *__restrict__ scatter) {
+    __syncwarp();
+    const unsigned long long e = lane < cnt ? q[lane] : 0ull;
+    const int64_t kk = (int64_t)(e >> kPointBits);
+    float c = 0.0f;
+    if (lane < cnt) {
+        const int s = (int)(e & ((1u << kPointBits) - 1));
+        const PairGeo P = pair_geo(__ldg(pairs + 2 * kk), __ldg(pairs + 2 * kk + 1), cpos, n_s, ncpr, nbpr, gb1);
+        const PointGeo Q = point_geo(P, spos, s);
+        c = point_term(P, Q, s, slow_angle(P, Q, t_cos), em, at, s_mu, t_g, t_eff, t_fk);
+    }
+    qv[lane] = c;
+    __syncwarp();
+    float cur = 0.0f;
+    if (lane < cnt && (lane == 0 || (int64_t)(q[lane - 1] >> kPointBits) != kk)) {
+        float sum = 0.0f;
+        for (int j = lane; j < cnt && (int64_t)(q[j] >> kPointBits) == kk; ++j) sum += qv[j];
+        if (kk == kcur) cur = sum;
+        else scatter[kk] += sum;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cur += __shfl_xor_sync(0xffffffffu, cur, o);  // one lane holds it
+    __syncwarp();
+    const int rest = qn - cnt;  // < 32 entries stay
+    const unsigned long long keep = lane < rest ? q[cnt + lane] : 0ull;
+    __syncwarp();
+    if (lane < rest) q[lane] = keep;
+    __syncwarp();
+    qn = rest;
+    return cur;
+}
+
+__global__ void __launch_bounds__(kBlock, 4)
 k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const float *__restrict__ cpos,
       const float *__restrict__ spos, int n_s, const float *__restrict__ em,
       const float *__restrict__ at, const float *__restrict__ umap, int u0, int u1, int u2,
       float us0, float us1, float us2, int ncpr, int nbpr, int gb1, const __grid_constant__ SssTables tab,
       float *__restrict__ scatter, float *__restrict__ scale) {
-    __shared__ float t_g[kAngles], t_eff[kAngles], t_fk[kAngles];
+    __shared__ float t_g[kAngles], t_eff[kAngles], t_fk[kAngles], t_cf[kAngles + 1];
     __shared__ double t_cos[kAngles];
+    __shared__ unsigned char t_start[kBuckets];
+    __shared__ unsigned long long s_q[kBlock / 32][kQueue];
+    __shared__ float s_qv[kBlock / 32][32];
     extern __shared__ float s_mu[];  // n_s entries: mu at the nearest voxel of each scatter point
     for (int t = threadIdx.x; t < n_s; t += blockDim.x) {
         // kn_formula.py:12-14; outside the map counts as 0
@@ -112,8 +278,14 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
         t_fk[t] = tab.fk[t];
         t_cos[t] = tab.cosd[t];
     }
+    for (int t = threadIdx.x; t <= kAngles; t += blockDim.x) t_cf[t] = tab.cosf_[t];
+    for (int t = threadIdx.x; t < kBuckets; t += blockDim.x) t_start[t] = tab.start[t];
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    unsigned long long *q = s_q[threadIdx.x >> 5];
+    float *qv = s_qv[threadIdx.x >> 5];
+    int qn = 0;  // queued items of this warp (warp-uniform)
+    const unsigned lt = (1u << lane) - 1u;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t k = warp; k < n_pairs; k += nwarps) {
@@ -122,83 +294,44 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
             if (lane == 0) { scatter[k] = 0.0f; scale[k] = 0.0f; }
             continue;
         }
-        const float ax = __ldg(cpos + 3 * a), ay = __ldg(cpos + 3 * a + 1), az = __ldg(cpos + 3 * a + 2);
-        const float bx = __ldg(cpos + 3 * b), by = __ldg(cpos + 3 * b + 1), bz = __ldg(cpos + 3 * b + 2);
-        // block normals at id / nbpr * 2 pi
-        float nax, nay, nbx, nby;
-        sincospif(2.0f * (float)block_id(ncpr, nbpr, gb1, ax, ay, az) / (float)nbpr, &nay, &nax);
-        sincospif(2.0f * (float)block_id(ncpr, nbpr, gb1, bx, by, bz) / (float)nbpr, &nby, &nbx);
-        const float dabx = bx - ax, daby = by - ay, dabz = bz - az;
-        const float ab2 = dabx * dabx + daby * daby + dabz * dabz;
-        // |AB| in double, squared again as the reference does (kn_formula.py:36-41)
-        const double Dab = sqrt((double)dabx * dabx + (double)daby * daby + (double)dabz * dabz);
-        const float ab = sqrtf(ab2);
-        const float *ema = em + (int64_t)a * n_s, *emb = em + (int64_t)b * n_s;
-        const float *ata = at + (int64_t)a * n_s, *atb = at + (int64_t)b * n_s;
+        PairGeo P = pair_geo(a, b, cpos, n_s, ncpr, nbpr, gb1);
         float acc = 0.0f;
-        for (int s = lane; s < n_s; s += 32) {
-            const float sx = __ldg(spos + 3 * s), sy = __ldg(spos + 3 * s + 1), sz = __ldg(spos + 3 * s + 2);
-            const float dax = ax - sx, day = ay - sy, daz = az - sz;
-            const float dbx = bx - sx, dby = by - sy, dbz = bz - sz;
-            const float as2 = dax * dax + day * day + daz * daz;
-            const float sb2 = dbx * dbx + dby * dby + dbz * dbz;
-            const float as = sqrtf(as2), sb = sqrtf(sb2);
-            const float den = 2.0f * as * sb;
-            float arg = -(as2 + sb2 - ab2) / den;
-            arg = fminf(1.0f, fmaxf(-1.0f, arg));
-            // |error of arg| <= 7u (as2 + sb2 + ab2) / den + 9u (u = 2^-24); acosf is within 5e-7
-            // rad and the degree conversion within 2.2e-5 degree
-            const float E = 5.0e-7f * (as2 + sb2 + ab2) / den + 6.0e-7f;
-            const float m = fabsf(arg) + E;
-            bool slow = m >= 0.9999f;
-            float deg = 0.0f;
-            if (!slow) {
-                deg = acosf(arg) * (float)(180.0 / M_PI);
-                const float tol = 4.0f * (57.2957795f * (E * rsqrtf(1.0f - m * m) + 5.0e-7f) + 2.2e-5f);
-                const float fr = deg - floorf(deg);
-                slow = fr < tol || fr > 1.0f - tol;
+        for (int s0 = 0; s0 < n_s; s0 += 32) {
+            const int s = s0 + lane;
+            const bool act = s < n_s;
+            PointGeo Q;
+            int ti = 0;
+            if (act) {
+                Q = point_geo(P, spos, s);
+                ti = fast_angle(P, Q, t_cf, t_start);
             }
-            int ti;
-            if (slow) {
-                // the cosine in double (as the reference) from the same float coordinates, then
-                // its whole degrees by comparison with cos(t deg): acos(x) >= t deg <=> x <= cos(t deg),
-                // starting from the FP32 estimate (no FP64 acos: FP64 issues at a small fraction
-                // of the FP32 rate here)
-                const double Dax = (double)ax - sx, Day = (double)ay - sy, Daz = (double)az - sz;
-                const double Dbx = (double)bx - sx, Dby = (double)by - sy, Dbz = (double)bz - sz;
-                const double Das = sqrt(Dax * Dax + Day * Day + Daz * Daz);
-                const double Dsb = sqrt(Dbx * Dbx + Dby * Dby + Dbz * Dbz);
-                double dargs = -(Das * Das + Dsb * Dsb - Dab * Dab) / (2 * Das * Dsb);
-                dargs = fmin(1.0, fmax(-1.0, dargs));
-                int t = min(max((int)(acosf((float)dargs) * (float)(180.0 / M_PI)), 0), kAngles - 1);
-                while (t < kAngles - 1 && dargs <= t_cos[t + 1]) ++t;
-                while (t > 0 && dargs > t_cos[t]) --t;
-                ti = t;
-            } else {
-                ti = (int)deg;
+            // undecided points are queued (qn < 32 here, so at most 63 entries)
+            const unsigned slow = __ballot_sync(0xffffffffu, act && ti < 0);
+            if (act && ti < 0) q[qn + __popc(slow & lt)] = ((unsigned long long)k << kPointBits) | (unsigned)s;
+            qn += __popc(slow);
+            if (act && ti >= 0) acc += point_term(P, Q, s, ti, em, at, s_mu, t_g, t_eff, t_fk);
+            if (qn >= 32) {
+                const float cur = flush_deferred(q, qv, qn, 32, k, lane, pairs, cpos, spos, n_s, em, at, ncpr,
+                                                 nbpr, gb1, s_mu, t_g, t_eff, t_fk, t_cos, scatter);
+                if (lane == 0) acc += cur;
+                // rebuilt rather than kept live across the flush (registers); flushes are rare
+                P = pair_geo(a, b, cpos, n_s, ncpr, nbpr, gb1);
             }
-            ti = min(max(ti, 0), kAngles - 1);
-            const float mu = s_mu[s];
-            const float gexp = t_g[ti];
-            const float a_a = __ldg(ata + s), a_b = __ldg(atb + s);
-            const float Ia = a_a * exp2f(__log2f(a_b) * gexp) * __ldg(ema + s);
-            const float Ib = exp2f(__log2f(a_a) * gexp) * a_b * __ldg(emb + s);
-            // area(S->A) uses A's block normal, area(S->B) B's; the divisions by |SA|, |SB| and
-            // their squares as multiplications by correctly rounded reciprocals
-            const float ias = __frcp_rn(as), isb = __frcp_rn(sb);
-            const float pa = (dax * nax + day * nay) * ias;
-            const float pb = (dbx * nbx + dby * nby) * isb;
-            acc += pa * t_eff[ti] * pb * (t_fk[ti] * mu) * (Ia + Ib) * (ias * ias) * (isb * isb);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) {
             scatter[k] = acc;
-            const float area = (dabx * nbx + daby * nby) / ab;
-            const float q = ab / area;
-            scale[k] = q * q;
+            const float dabx = P.bx - P.ax, daby = P.by - P.ay;
+            const float ab = sqrtf(P.ab2);
+            const float area = (dabx * P.nbx + daby * P.nby) / ab;
+            const float qq = ab / area;
+            scale[k] = qq * qq;
         }
     }
+    if (qn > 0)
+        flush_deferred(q, qv, qn, qn, -1, lane, pairs, cpos, spos, n_s, em, at, ncpr, nbpr, gb1, s_mu, t_g,
+                       t_eff, t_fk, t_cos, scatter);
 }
 
 }  // namespace srf

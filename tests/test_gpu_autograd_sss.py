@@ -112,6 +112,41 @@ def test_sss_kernel_matches_oracle(cuda_lib, oracle):
     np.testing.assert_allclose(sl[ok], ref_c[ok], rtol=1e-5)
 
 
+def test_sss_kernel_many_undecided_angles(cuda_lib, oracle):
+    """Scatter points on the segment between two crystals (scattering angle 0, cosine 1) put 80
+    points of one pair on the double-precision angle path, so that pair's queued evaluations are
+    drained while it is still being summed; other pairs queue a few each."""
+    import os
+    from srf_gb300 import kernels
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "sss.npz")))
+    c = g["crystal"]
+    a0 = int(np.argmin(np.abs(c[:, 2])))
+    u = c[:, :2] / np.linalg.norm(c[:, :2], axis=1, keepdims=True)
+    score = u @ u[a0] + 0.01 * np.abs(c[:, 2] - c[a0, 2])
+    b0 = int(np.argmin(score))  # about opposite a0, at a similar z
+    t = np.linspace(0.25, 0.75, 80, dtype=np.float64)[:, None]
+    line = (c[a0] + t * (c[b0].astype(np.float64) - c[a0])).astype(np.float32)
+    rng = np.random.default_rng(11)
+    spos = np.vstack([g["scatter"], line, rng.uniform([-60, -60, -14], [60, 60, 14], (8, 3))]).astype(np.float32)
+    n_s = len(spos)
+    sumup = rng.uniform(0.5, 2.0, (len(c), n_s)).astype(np.float32)
+    atten = rng.uniform(0.2, 1.0, (len(c), n_s)).astype(np.float32)
+    pairs = np.vstack([[[a0, b0]] * 3, [[b0, a0]], g["pairs"], rng.integers(0, len(c), (500, 2))]).astype(np.int32)
+    pairs = pairs[pairs[:, 0] != pairs[:, 1]]
+    args = (g["umap"], g["usize"], int(g["ncpr"]), int(g["nbpr"]), g["grid_block"], int(g["low"]),
+            int(g["high"]), float(g["res"]))
+    ref_s, _ = oracle.sss(pairs, c, spos, sumup, atten, *args)
+    dev = torch.device("cuda", 0)
+    d = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to(dev)
+    sc, _ = kernels.sss(d(pairs), d(c), d(spos), d(sumup), d(atten), d(g["umap"]), list(g["usize"]),
+                        int(g["ncpr"]), int(g["nbpr"]), list(g["grid_block"]), int(g["low"]),
+                        int(g["high"]), float(g["res"]))
+    sc = sc.cpu().numpy()
+    assert ref_s[0] > 0
+    np.testing.assert_allclose(sc[:4], ref_s[:4], rtol=2e-5)  # the collinear pair, both orders
+    np.testing.assert_allclose(sc, ref_s, rtol=2e-5, atol=1e-6 * np.abs(ref_s).max())
+
+
 def test_scatter_correct_pipeline_matches_oracle(cuda_lib, oracle, small_case):
     import srf_gb300 as nef
     from srf_gb300 import scatter as S

@@ -125,3 +125,39 @@ def test_osem_tof_additive_term_matches_oracle(cuda_lib, oracle, small_case, ema
                       tof_nsigma=3.0, add=add)
     assert rel_l2(out.data, ref) <= TOL
     assert rel_l2(out.data, none.data) > 1e-4  # the term matters
+
+
+@pytest.mark.parametrize("shape,offset", [((36, 20, 3), 0), ((36, 20, 3), 1), ((37, 21, 2), 0), ((200, 200, 2), 0)])
+def test_osem_update_paths_bit_exact(cuda_lib, shape, offset):
+    """srf_osem_update on both of its kernels: 16-byte accesses (nx, ny multiples of 4, aligned
+    arrays) and the scalar tile kernel (odd sizes, or arrays one float off alignment). Both are
+    x * (bp + bp_t) / emap in FP32 with emap zeros -> 1e8, x_t the transposed copy, both
+    accumulators zeroed; compared bit for bit with numpy's FP32 arithmetic."""
+    import torch
+    from srf_gb300._lib import call, i32, i32x3, ptr, stream_ptr
+    nx, ny, nz = shape
+    v = nx * ny * nz
+    rng = np.random.default_rng(nx * 131 + offset)
+    x = rng.uniform(0.5, 2.0, (nz, ny, nx)).astype(np.float32)
+    bp = rng.uniform(0.0, 3.0, (nz, ny, nx)).astype(np.float32)
+    bpt = rng.uniform(0.0, 3.0, (nz, nx, ny)).astype(np.float32)
+    em = rng.uniform(0.5, 1.5, (nz, ny, nx)).astype(np.float32)
+    em[rng.random(em.shape) < 0.1] = 0.0
+    dev = torch.device("cuda", 0)
+
+    def put(a):
+        buf = torch.zeros(v + offset, dtype=torch.float32, device=dev)
+        buf[offset:] = torch.as_tensor(a.reshape(-1), device=dev)
+        return buf[offset:]
+
+    dx, dxt, dbp, dbpt, dem = put(x), put(np.ascontiguousarray(x.transpose(0, 2, 1))), put(bp), put(bpt), put(em)
+    call("srf_osem_update", ptr(dx), ptr(dxt), ptr(dbp), ptr(dbpt), ptr(dem), i32(1), i32x3(shape),
+         stream_ptr(dev))
+    b = bp + bpt.transpose(0, 2, 1)
+    e = np.where(em == 0.0, np.float32(1e8), em)
+    want = (x * b) / e
+    got = dx.cpu().numpy().reshape(nz, ny, nx)
+    assert np.array_equal(got.view(np.int32), want.view(np.int32))
+    got_t = dxt.cpu().numpy().reshape(nz, nx, ny)
+    assert np.array_equal(got_t.view(np.int32), np.ascontiguousarray(want.transpose(0, 2, 1)).view(np.int32))
+    assert not dbp.any().item() and not dbpt.any().item()
