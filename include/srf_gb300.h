@@ -303,7 +303,7 @@ int srf_emap_block_full(const float *crystal_table, int32_t n_blocks, int32_t m,
  * the angle inside fkn):
  *   pairs          int32 (a, b) crystal ids, n_pairs rows
  *   crystal_pos    float32 (n_crystals, 3); scatter_pos float32 (n_scatter, 3), n_scatter <= 12288
- *   sumup_emission, atten  float32 (n_crystals, n_scatter), crystal-major
+ *   sumup_emission, atten  float32 (n_crystals, n_scatter), crystal-major, n_crystals * n_scatter < 2^31
  *   umap           float32 (shape0, shape1, shape2) C order, umap_size mm
  * Outputs scatter[k] and scale[k] before the host scaling of scatter_fraction.py:27-36. */
 int srf_sss(const int32_t *pairs, int64_t n_pairs, const float *crystal_pos, int32_t n_crystals,

@@ -61,13 +61,13 @@ __device__ __forceinline__ int block_id(int ncpr, int nbpr, int gb1, float px, f
 
 // Per whole-degree angle: 511 / E' (the attenuation exponent), eff(E') and the Klein-Nishina factor
 // as the reference evaluates it (fkn receives the angle). Built on the host in double and rounded
-// to float, once per call, and passed by value (8.5 KB of kernel parameters). Whole degrees of
+// to float, once per call, and passed by value (7.7 KB of kernel parameters). Whole degrees of
 // acos(x) are max{t : x <= cos(t deg)}; `start` gives, for each of kBuckets equal slices of
 // [-1, 1] in x, that t at the slice's upper end, from which a search over the cos table begins.
 constexpr int kBuckets = 4096;
 struct SssTables {
-    float g[kAngles], eff[kAngles], fk[kAngles];
-    float cosf_[kAngles + 1];  // cos(t deg) rounded to float; [kAngles] = -2, below every cosine
+    float2 ge[kAngles];        // (511 / E', eff(E') * fkn), the factors of a term at t degrees
+    float cosf_[kAngles + 2];  // cos(t deg) rounded to float; [kAngles..] = -2, below every cosine
     double cosd[kAngles];      // cos(t deg) in double
     unsigned char start[kBuckets];
 };
@@ -83,16 +83,15 @@ static SssTables sss_tables(int low, int high, double res) {
         const double a = ang;  // the reference's fkn receives the angle
         const double diff = 1.0 / ((2.0 - a) * (2.0 - a)) * ((1.0 + a * a) / 2.0 + (1.0 - a) * (1.0 - a) / 2.0 / (2.0 - a));
         const double sigma = M_PI * (40.0 / 9.0 - 3.0 * std::log(3.0));
-        T.g[t] = (float)(511.0 / e_sc);
-        T.eff[t] = (float)eff;
-        T.fk[t] = (float)(diff / sigma);
+        T.ge[t] = make_float2((float)(511.0 / e_sc), (float)(eff * (diff / sigma)));
         T.cosd[t] = c;
     }
     T.cosd[kAngles - 1] = -1.0;
     for (int t = 0; t < kAngles; ++t) T.cosf_[t] = (float)T.cosd[t];
-    T.cosf_[kAngles] = -2.0f;
+    T.cosf_[kAngles] = T.cosf_[kAngles + 1] = -2.0f;
     for (int b = 0; b < kBuckets; ++b) {
-        const double hi = std::min(1.0, -1.0 + 2.0 * (b + 1) / kBuckets);
+        // a little above the slice (the float bucket index may round down)
+        const double hi = std::min(1.0, -1.0 + 2.0 * (b + 1) / kBuckets + 1e-6);
         int t = (int)std::floor(std::acos(hi) * 180.0 / M_PI);
         T.start[b] = (unsigned char)std::min(std::max(t, 0), kAngles - 1);
     }
@@ -104,7 +103,7 @@ struct PairGeo {
     float ax, ay, az, bx, by, bz;
     float nax, nay, nbx, nby;  // block normals of A and B
     float ab2;                 // |AB|^2 in FP32
-    int64_t ra, rb;            // offsets of A's and B's rows of the per-point tables
+    int ra, rb;                // offsets of A's and B's rows of the per-point tables (< 2^31)
 };
 
 __device__ __forceinline__ PairGeo pair_geo(int a, int b, const float *__restrict__ cpos, int n_s, int ncpr, int nbpr, int gb1) {
@@ -116,7 +115,7 @@ __device__ __forceinline__ PairGeo pair_geo(int a, int b, const float *__restric
     sincospif(2.0f * (float)block_id(ncpr, nbpr, gb1, P.bx, P.by, P.bz) / (float)nbpr, &P.nby, &P.nbx);
     const float dabx = P.bx - P.ax, daby = P.by - P.ay, dabz = P.bz - P.az;
     P.ab2 = dabx * dabx + daby * daby + dabz * dabz;
-    P.ra = (int64_t)a * n_s; P.rb = (int64_t)b * n_s;
+    P.ra = a * n_s; P.rb = b * n_s;
     return P;
 }
 
@@ -156,10 +155,19 @@ __device__ __forceinline__ int fast_angle(const PairGeo &P, const PointGeo &Q, c
     arg = fminf(1.0f, fmaxf(-1.0f, arg));
     const float Em = 4.0f * 1.32e-6f * S * iden + 4.0e-8f;
     const int b = min(max((int)((arg + 1.0f) * (0.5f * kBuckets)), 0), kBuckets - 1);
+    // t from the slice's start: at most two whole degrees lie in one slice (three steps cover
+    // its widened upper end); a start above arg's angle, or more steps, goes to the double path
     int t = t_start[b];
-    while (t < kAngles - 1 && arg <= t_cf[t + 1]) ++t;
-    while (t > 0 && arg > t_cf[t]) --t;
-    if (t_cf[t] - arg <= Em || arg - t_cf[t + 1] <= Em) return -1;
+    float hi = t_cf[t], lo = t_cf[t + 1];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const bool up = arg <= lo;
+        t += up ? 1 : 0;
+        hi = up ? lo : hi;
+        lo = t_cf[t + 1];
+    }
+    if (arg > hi || arg <= lo) return -1;
+    if (hi - arg <= Em || arg - lo <= Em) return -1;
     return t;
 }
 
@@ -183,20 +191,26 @@ __device__ __forceinline__ int slow_angle(const PairGeo &P, const PointGeo &Q, c
 }
 
 // The term of scatter point s at whole-degree angle ti (FP32).
+__device__ __forceinline__ float ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ float point_term(const PairGeo &P, const PointGeo &Q, int s, int ti,
                                             const float *__restrict__ em, const float *__restrict__ at,
-                                            const float *s_mu, const float *t_g, const float *t_eff,
-                                            const float *t_fk) {
-    const float gexp = t_g[ti];
+                                            const float *s_mu, const float2 *t_ge) {
+    const float2 ge = t_ge[ti];
     const float a_a = __ldg(at + P.ra + s), a_b = __ldg(at + P.rb + s);
-    const float Ia = a_a * exp2f(__log2f(a_b) * gexp) * __ldg(em + P.ra + s);
-    const float Ib = exp2f(__log2f(a_a) * gexp) * a_b * __ldg(em + P.rb + s);
+    // atten^(511/E') as 2^(log2(atten) * 511/E'), both approximate (relative error ~1e-6)
+    const float Ia = a_a * ex2(__log2f(a_b) * ge.x) * __ldg(em + P.ra + s);
+    const float Ib = ex2(__log2f(a_a) * ge.x) * a_b * __ldg(em + P.rb + s);
     // area(S->A) uses A's block normal, area(S->B) B's; the divisions by |SA|, |SB| and their
     // squares as multiplications by the reciprocal square roots of |SA|^2, |SB|^2
     const float ias = Q.ias, isb = Q.isb;
     const float pa = (Q.dax * P.nax + Q.day * P.nay) * ias;
     const float pb = (Q.dbx * P.nbx + Q.dby * P.nby) * isb;
-    return pa * t_eff[ti] * pb * (t_fk[ti] * s_mu[s]) * (Ia + Ib) * (ias * ias) * (isb * isb);
+    return pa * ge.y * pb * s_mu[s] * (Ia + Ib) * (ias * ias) * (isb * isb);
 }
 
 // Deferred double-precision angles: a warp queues the (pair, point) items whose FP32 angle is
@@ -216,7 +230,7 @@ __device__ __forceinline__ float flush_deferred(unsigned long long *q, float *qv
                                                const float *__restrict__ spos, int n_s,
                                                const float *__restrict__ em, const float *__restrict__ at,
                                                int ncpr, int nbpr, int gb1, const float *s_mu,
-                                               const float *t_g, const float *t_eff, const float *t_fk,
+                                               const float2 *t_ge,
                                                const double *t_cos, float *__restrict__ scatter) {
     __syncwarp();
     const unsigned long long e = lane < cnt ? q[lane] : 0ull;
@@ -226,7 +240,7 @@ __device__ __forceinline__ float flush_deferred(unsigned long long *q, float *qv
         const int s = (int)(e & ((1u << kPointBits) - 1));
         const PairGeo P = pair_geo(__ldg(pairs + 2 * kk), __ldg(pairs + 2 * kk + 1), cpos, n_s, ncpr, nbpr, gb1);
         const PointGeo Q = point_geo(P, spos, s);
-        c = point_term(P, Q, s, slow_angle(P, Q, t_cos), em, at, s_mu, t_g, t_eff, t_fk);
+        c = point_term(P, Q, s, slow_angle(P, Q, t_cos), em, at, s_mu, t_ge);
     }
     qv[lane] = c;
     __syncwarp();
@@ -249,17 +263,22 @@ __device__ __forceinline__ float flush_deferred(unsigned long long *q, float *qv
     return cur;
 }
 
-__global__ void __launch_bounds__(kBlock, 4)
+// 128-thread blocks, 7 per SM: 72 registers without spills (256-thread blocks at 4 per SM forced
+// 64 with spills in the point loop, at 3 per SM 24 warps; both measured slower)
+constexpr int kSssBlock = 128;
+
+__global__ void __launch_bounds__(kSssBlock, 7)
 k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const float *__restrict__ cpos,
       const float *__restrict__ spos, int n_s, const float *__restrict__ em,
       const float *__restrict__ at, const float *__restrict__ umap, int u0, int u1, int u2,
       float us0, float us1, float us2, int ncpr, int nbpr, int gb1, const __grid_constant__ SssTables tab,
       float *__restrict__ scatter, float *__restrict__ scale) {
-    __shared__ float t_g[kAngles], t_eff[kAngles], t_fk[kAngles], t_cf[kAngles + 1];
+    __shared__ float2 t_ge[kAngles];
+    __shared__ float t_cf[kAngles + 2];
     __shared__ double t_cos[kAngles];
     __shared__ unsigned char t_start[kBuckets];
-    __shared__ unsigned long long s_q[kBlock / 32][kQueue];
-    __shared__ float s_qv[kBlock / 32][32];
+    __shared__ unsigned long long s_q[kSssBlock / 32][kQueue];
+    __shared__ float s_qv[kSssBlock / 32][32];
     extern __shared__ float s_mu[];  // n_s entries: mu at the nearest voxel of each scatter point
     for (int t = threadIdx.x; t < n_s; t += blockDim.x) {
         // kn_formula.py:12-14; outside the map counts as 0
@@ -273,12 +292,10 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
         s_mu[t] = mu;
     }
     for (int t = threadIdx.x; t < kAngles; t += blockDim.x) {
-        t_g[t] = tab.g[t];
-        t_eff[t] = tab.eff[t];
-        t_fk[t] = tab.fk[t];
+        t_ge[t] = tab.ge[t];
         t_cos[t] = tab.cosd[t];
     }
-    for (int t = threadIdx.x; t <= kAngles; t += blockDim.x) t_cf[t] = tab.cosf_[t];
+    for (int t = threadIdx.x; t < kAngles + 2; t += blockDim.x) t_cf[t] = tab.cosf_[t];
     for (int t = threadIdx.x; t < kBuckets; t += blockDim.x) t_start[t] = tab.start[t];
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -309,10 +326,10 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
             const unsigned slow = __ballot_sync(0xffffffffu, act && ti < 0);
             if (act && ti < 0) q[qn + __popc(slow & lt)] = ((unsigned long long)k << kPointBits) | (unsigned)s;
             qn += __popc(slow);
-            if (act && ti >= 0) acc += point_term(P, Q, s, ti, em, at, s_mu, t_g, t_eff, t_fk);
+            if (act && ti >= 0) acc += point_term(P, Q, s, ti, em, at, s_mu, t_ge);
             if (qn >= 32) {
                 const float cur = flush_deferred(q, qv, qn, 32, k, lane, pairs, cpos, spos, n_s, em, at, ncpr,
-                                                 nbpr, gb1, s_mu, t_g, t_eff, t_fk, t_cos, scatter);
+                                                 nbpr, gb1, s_mu, t_ge, t_cos, scatter);
                 if (lane == 0) acc += cur;
                 // rebuilt rather than kept live across the flush (registers); flushes are rare
                 P = pair_geo(a, b, cpos, n_s, ncpr, nbpr, gb1);
@@ -330,8 +347,8 @@ k_sss(const int32_t *__restrict__ pairs, int64_t n_pairs, int n_crystals, const 
         }
     }
     if (qn > 0)
-        flush_deferred(q, qv, qn, qn, -1, lane, pairs, cpos, spos, n_s, em, at, ncpr, nbpr, gb1, s_mu, t_g,
-                       t_eff, t_fk, t_cos, scatter);
+        flush_deferred(q, qv, qn, qn, -1, lane, pairs, cpos, spos, n_s, em, at, ncpr, nbpr, gb1, s_mu, t_ge,
+                       t_cos, scatter);
 }
 
 }  // namespace srf
@@ -360,10 +377,12 @@ extern "C" int srf_sss(const int32_t *pairs, int64_t n_pairs, const float *cryst
     if (!std::isfinite(resolution) || !(resolution > 0)) return fail(SRF_ENONFINITE, "resolution must be > 0");
     if (high_energy - low_energy > 5 * 100000) return fail(SRF_ERANGE, "energy window too wide");
     if (n_scatter > kMaxScatterPoints) return fail(SRF_ERANGE, "at most %d scatter points", kMaxScatterPoints);
+    if ((int64_t)n_crystals * n_scatter >= (int64_t(1) << 31))
+        return fail(SRF_ERANGE, "n_crystals * n_scatter must be below 2^31");
     const double res = sqrt(511.0) * (double)resolution;
     const int smem = n_scatter * (int)sizeof(float);
-    unsigned blocks = grid_for(k_sss, n_pairs, kBlock / 32, smem);
-    k_sss<<<blocks, kBlock, smem, (cudaStream_t)stream>>>(
+    unsigned blocks = grid_for(k_sss, n_pairs, kSssBlock / 32, smem, kSssBlock);
+    k_sss<<<blocks, kSssBlock, smem, (cudaStream_t)stream>>>(
         pairs, n_pairs, n_crystals, crystal_pos, scatter_pos, n_scatter, sumup_emission, atten, umap,
         umap_shape[0], umap_shape[1], umap_shape[2], umap_size[0], umap_size[1], umap_size[2],
         nb_crystals_per_ring, nb_blocks_per_ring, grid_block[1], sss_tables(low_energy, high_energy, res),

@@ -23,7 +23,7 @@ from typing import Dict, Tuple
 import numpy as np
 import torch
 
-from . import kernels
+from . import _lib, kernels
 from .geometry import EcatIndexToCrystalPos, ImageConfig, PetEcatScanner
 
 VIEWS, RADIAL, PLANES = 312, 52, 52
@@ -173,10 +173,13 @@ def sss_pairs(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor, cpo
     m, k = cpos.shape[0], sp.shape[0]
     Ld = torch.cat([cpos[:, None, :].expand(m, k, 3), sp[None, :, :].expand(m, k, 3)], 2).reshape(-1, 6)
     Ld = Ld.contiguous()
-    p = kernels.project(Ld, kernels.xfast(emission), ic.center, ic.size)
+    # detector -> scatter point LORs cross at most 64 slabs of the 64 x 64 x 32 grid: 8 lanes per
+    # LOR beat the default 32 (measured 6.5 -> 5.1 ms for the whole coarse sinogram)
+    with _lib.tuning(8, 2):
+        p = kernels.project(Ld, kernels.xfast(emission), ic.center, ic.size)
+        atten = kernels.attenuation(Ld, kernels.xfast(mu), ic.center, ic.size).reshape(m, k)
     len2 = ((Ld[:, 3] - Ld[:, 0]) ** 2 + (Ld[:, 4] - Ld[:, 1]) ** 2 + (Ld[:, 5] - Ld[:, 2]) ** 2)
     sumup = (p * len2).reshape(m, k)
-    atten = kernels.attenuation(Ld, kernels.xfast(mu), ic.center, ic.size).reshape(m, k)
     s = geo.scanner
     sc, _ = kernels.sss(pairs.contiguous(), cpos.contiguous(), sp, sumup.contiguous(), atten.contiguous(),
                         mu.contiguous(), list(ic.size), s.nb_blocks_per_ring * s.blocks.shape[1],
