@@ -403,6 +403,8 @@ def run_batched(a, ws, rank, local):
             "s_per_iter_graph_concurrent_study_chains": graph_concurrent_s,
             "s_per_iter_all_studies_eager_batch": eager_s,
             "s_per_iter_sum_of_single_studies": float(sum(per_study)),
+            # every study at the best single-study visit rate: what no batching can beat
+            "s_per_iter_ceiling_best_single_rate": total_visits / max(v / t for v, t in zip(visits, per_study)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded phantoms per study)",
             "config": {"workload": "batched_uneven_studies", "studies": len(studies),
@@ -787,10 +789,23 @@ def run_surrogate(a, ws, rank, local):
         t_sss.append(ts)
         t_sur.append(tc)
     clk = clocks.stop()
-    study = ScatterStudy(geo, seeds[0], n_trues=int(min(a.events, 2e6)))
+    # the OSEM image on every held-out phantom: SSS scatter against the corrected network estimate
+    # (what the network path gives), and against what the guard returns (SSS on a fallback)
+    rel = lambda u, v: float((torch.linalg.vector_norm(u - v) / torch.linalg.vector_norm(v)).item())
+    img_net, img_guard, img_none, fb5 = [], [], [], 0
+    study = None
+    for sd in seeds:
+        st_ = ScatterStudy(geo, sd, n_trues=int(min(a.events, 2e6)))
+        study = study or st_
+        i_sss = st_.reconstruct(st_.sss)
+        est, info = sur.estimate(st_.emission, st_.mu, fallback=False)
+        e_net = rel(st_.reconstruct(est), i_sss)
+        img_net.append(e_net)
+        img_guard.append(0.0 if info["spot_rel_l2"] > sur.fallback_tol else e_net)
+        img_none.append(rel(st_.x0, i_sss))
+        fb5 += int(info["spot_rel_l2"] > 0.05)
     img_sss = study.reconstruct(study.sss)
     img_sur = study.reconstruct(sur.estimate(study.emission, study.mu, fallback=False)[0])
-    rel = lambda u, v: float((torch.linalg.vector_norm(u - v) / torch.linalg.vector_norm(v)).item())
     med_sss, med_sur, med_net = statistics.median(t_sss), statistics.median(t_sur), statistics.median(t_net)
     mean_sss, mean_sur = sum(t_sss) / len(t_sss), sum(t_sur) / len(t_sur)
     if rank == 0:
@@ -815,10 +830,15 @@ def run_surrogate(a, ws, rank, local):
             "sinogram_rel_l2_corrected_max": max(cerrs),
             "spot_rel_l2_mean": sum(spot) / len(spot),
             "spot_rel_l2_uncorrected_mean": sum(spot_raw) / len(spot_raw), "fallbacks": fallbacks,
+            "fallbacks_at_5pct_spot": fb5,
             "osem": {"events": int(study.events.shape[0]), "scatter_fraction": study.sf,
                      "iterations": study.n_iter, "subsets": study.n_sub,
                      "image_rel_l2_surrogate_vs_sss": rel(img_sur, img_sss),
-                     "image_rel_l2_uncorrected_vs_sss": rel(study.x0, img_sss)},
+                     "image_rel_l2_uncorrected_vs_sss": rel(study.x0, img_sss),
+                     "held_out_image_rel_l2_network_mean": sum(img_net) / len(img_net),
+                     "held_out_image_rel_l2_network_max": max(img_net),
+                     "held_out_image_rel_l2_guarded_max": max(img_guard),
+                     "held_out_image_rel_l2_uncorrected_min": min(img_none)},
             "clocks": clk,
         }), flush=True)
 

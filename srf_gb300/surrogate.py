@@ -265,6 +265,7 @@ def load_weights(path: str, device="cuda") -> Tuple[UNet3D, Dict[str, float]]:
 
 
 DEFAULT_WEIGHTS = __file__.rsplit("/", 1)[0] + "/weights/scatter_unet.npz"
+DEFAULT_GUARD = __file__.rsplit("/", 1)[0] + "/weights/scatter_guard.json"
 
 
 # ---------------------------------------------------------------- surrogate with SSS as the judge
@@ -380,8 +381,16 @@ class ScatterSurrogate:
         return pools
 
     @classmethod
-    def load(cls, geo, path: str = DEFAULT_WEIGHTS, **kw) -> "ScatterSurrogate":
+    def load(cls, geo, path: str = DEFAULT_WEIGHTS, guard: Optional[str] = DEFAULT_GUARD,
+             **kw) -> "ScatterSurrogate":
+        """The network from ``path``; the fallback threshold from the guard calibration file
+        ``guard`` (see calibrate_guard) unless ``fallback_tol`` is given."""
+        import json
+        import os
         net, meta = load_weights(path, geo.device)
+        if "fallback_tol" not in kw and guard is not None and os.path.exists(guard):
+            with open(guard) as f:
+                kw["fallback_tol"] = float(json.load(f)["fallback_tol"])
         return cls(geo, net, meta["target_scale"], **kw)
 
     def _predict_eager(self, emission: torch.Tensor, mu: torch.Tensor) -> torch.Tensor:
@@ -565,8 +574,47 @@ def evaluate(sur: "ScatterSurrogate", seeds) -> List[float]:
     return errs
 
 
+def guard_threshold(records, image_target: float, margin: float) -> float:
+    """The largest spot-check difference s such that every calibration study whose judged spot
+    difference is at most s kept its OSEM image within margin * image_target of the SSS-corrected
+    image (records: (spot_rel_l2, image_rel_l2) pairs). Never above the largest difference seen;
+    below the smallest when even that study missed the bound (then everything falls back)."""
+    bound = margin * image_target
+    tol = None
+    for spot, img in sorted(records):
+        if img > bound:
+            break
+        tol = spot
+    if tol is None:
+        return 0.0
+    return float(tol)
+
+
+def calibrate_guard(sur: "ScatterSurrogate", seeds, image_target: float = 0.01, margin: float = 0.75,
+                    n_trues: int = 2_000_000, log=None) -> Dict:
+    """Calibrate the fallback threshold on the OSEM image, the quantity the surrogate must keep
+    within ``image_target`` of SSS: for each calibration phantom (seeds apart from the training and
+    held-out ones) a ScatterStudy is reconstructed with SSS scatter and with the corrected network
+    estimate, and the image difference is paired with the spot check's judged difference."""
+    from .scatter_sinogram import ScatterStudy
+    recs = []
+    for sd in seeds:
+        study = ScatterStudy(sur.geo, int(sd), n_trues=n_trues)
+        est, info = sur.estimate(study.emission, study.mu, fallback=False)
+        img_sss = study.reconstruct(study.sss)
+        img_sur = study.reconstruct(est)
+        err = float((torch.linalg.vector_norm(img_sur - img_sss) / torch.linalg.vector_norm(img_sss)).item())
+        recs.append({"seed": int(sd), "spot_rel_l2": float(info["spot_rel_l2"]), "image_rel_l2": err})
+        if log:
+            log(f"seed {sd}: spot {info['spot_rel_l2']:.4f} image {err:.5f}")
+    tol = guard_threshold([(r["spot_rel_l2"], r["image_rel_l2"]) for r in recs], image_target, margin)
+    return {"fallback_tol": tol, "image_target": image_target, "margin": margin, "n_trues": n_trues,
+            "studies": recs}
+
+
 def main(argv=None) -> None:
-    """python -m srf_gb300.surrogate --out weights.npz [--train 2000 --held-out 200 --epochs N]"""
+    """python -m srf_gb300.surrogate --out weights.npz [--train 2000 --held-out 200 --epochs N]
+    python -m srf_gb300.surrogate --calibrate guard.json [--studies 40]"""
     import argparse
     import json
     import time
@@ -580,10 +628,20 @@ def main(argv=None) -> None:
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--channels", default="32,64,96")
+    ap.add_argument("--calibrate", default=None, help="write the guard calibration to this file")
+    ap.add_argument("--studies", type=int, default=40, help="calibration phantoms")
     a = ap.parse_args(argv)
     log = lambda m: print(f"[{time.strftime('%H:%M:%S')}] {m}", flush=True)
     dev = torch.device("cuda", 0)
     geo = CoarseGeometry(synth.scanner_clinical(), device=dev)
+    if a.calibrate:
+        # calibration phantoms: seeds 3,000,000 + i (training uses 0.., held-out 1,000,000 + i)
+        sur = ScatterSurrogate.load(geo, a.out, guard=None)
+        rec = calibrate_guard(sur, range(3_000_000, 3_000_000 + a.studies), log=log)
+        with open(a.calibrate, "w") as f:
+            json.dump(rec, f, indent=1)
+        log(f"fallback_tol {rec['fallback_tol']:.4f}")
+        return
     t0 = time.time()
     X, T, scales = build_dataset(geo, range(a.train), log)
     torch.cuda.synchronize()

@@ -203,3 +203,14 @@ def test_surrogate_correction_basis_and_fit():
     assert judged < 1e-5 and raw > 0.05
     e0, _, _ = spot_fit(np.zeros(phi.shape[1]), bins[:16], rng.uniform(size=16), phi)
     assert np.array_equal(e0, np.eye(9)[0])
+
+
+def test_surrogate_guard_threshold_rule():
+    """The fallback threshold is the largest calibration spot difference below which every
+    study kept its OSEM image within margin * target; never above what was observed."""
+    from srf_gb300.surrogate import guard_threshold
+    recs = [(0.03, 0.002), (0.05, 0.004), (0.08, 0.007), (0.09, 0.0085), (0.12, 0.006)]
+    assert guard_threshold(recs, 0.01, 0.75) == 0.08      # the 0.09 study breaks 0.75 %
+    assert guard_threshold(recs, 0.01, 1.0) == 0.12       # all within 1 %: the largest seen
+    assert guard_threshold([(0.02, 0.02)], 0.01, 0.75) == 0.0
+    assert guard_threshold([], 0.01, 0.75) == 0.0
