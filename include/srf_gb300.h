@@ -330,6 +330,12 @@ int srf_calib_sink_size(void);
  * yf (optional) receives the FP32 values. Runs on the tensor cores (mma.sync BF16). */
 int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *w, const float *bias,
                    int32_t cout, int32_t relu, void *y, const int32_t ys[6], float *yf, void *stream);
+/* on != 0: 128-voxel x 32-channel tiles of srf_conv3d_fwd run on tcgen05.mma (accumulator in
+ * tensor memory) instead of mma.sync; process-wide, read at launch. */
+int srf_set_conv_tc(int32_t on);
+/* *status = 1 if a tcgen05 convolution gave up waiting for its tensor-core work (bounded waits),
+ * else 0. Synchronises with the device. */
+int srf_conv_tc_status(int32_t *status);
 /* dw[co][tap][ci] += sum_v dy[v, co] x[v + tap - 1, ci] (FP32 accumulation). */
 int srf_conv3d_wgrad(const void *x, const int32_t xs[6], int32_t cin, const void *dy, const int32_t ds[6],
                      int32_t cout, float *dw, void *stream);

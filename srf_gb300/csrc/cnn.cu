@@ -192,6 +192,203 @@ k_conv3d_fwd(const __nv_bfloat16 *__restrict__ x, Act xa, int cin, const __nv_bf
     }
 }
 
+// ---------------------------------------------------------------- tcgen05 variant
+// The 128-voxel x 32-channel tile on the 5th-generation tensor cores: each (tap, 16-channel) K
+// step's gathered input rows (A, 128 x 16) and weight slice (B, 32 x 16) are written into one of
+// kTcStages shared-memory stages in the canonical no-swizzle K-major layout (8-row x 16-byte core
+// matrices; K-adjacent core matrices 128 B apart, 8-row groups 256 B apart); one thread issues
+// tcgen05.mma (kind::f16, BF16 inputs, FP32 accumulator in tensor memory, M = 128, N = 32) and
+// commits it to the stage's mbarrier, which the threads wait on before refilling that stage.
+// The next step's global loads are in flight meanwhile. The accumulator (128 lanes x 32 columns
+// of TMEM) is read back with tcgen05.ld for the bias/activation epilogue. Every wait is bounded:
+// on a timeout the kernel records it in g_tc_status, waits (bounded) for its last commit, frees
+// its tensor memory and returns.
+constexpr int kTcStages = 4;
+constexpr int kTcM = 128, kTcN = 32;
+constexpr int kTcABytes = kTcM * kCK * 2, kTcBBytes = kTcN * kCK * 2;  // 4096, 1024
+constexpr uint32_t kTcCols = 32;                                       // TMEM columns (FP32 N)
+constexpr int kTcSpin = 1 << 20;                                       // mbarrier polls before giving up
+
+__device__ int g_tc_status;  // 0, or 1 when a tcgen05 conv launch gave up waiting
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int i = 0; i < kTcSpin; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Shared-memory matrix descriptor (no swizzle, K-major): start address, leading (K-direction)
+// and stride (8-row direction) byte offsets, all >> 4; bit 46 set (descriptor version).
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B (bits 7-9,
+// 10-12 = 1), both K-major, N >> 3 in bits 17-22, M >> 4 in bits 24-28.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                              ((uint32_t)(kTcM >> 4) << 24);
+
+__global__ void __launch_bounds__(128, 4)
+k_conv3d_fwd_tc(const __nv_bfloat16 *__restrict__ x, Act xa, int cin, const __nv_bfloat16 *__restrict__ wt,
+                const float *__restrict__ bias, int cout, int relu, __nv_bfloat16 *__restrict__ y, Act ya,
+                float *__restrict__ yf) {
+    __shared__ __align__(1024) unsigned char sA[kTcStages][kTcABytes];
+    __shared__ __align__(1024) unsigned char sB[kTcStages][kTcBBytes];
+    __shared__ __align__(8) uint64_t bars[kTcStages];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int gave_up;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int64_t nvox = (int64_t)xa.d * xa.h * xa.w;
+    const int64_t v0 = (int64_t)blockIdx.x * kTcM;
+    const int co0 = blockIdx.y * kTcN;
+    const int nb = blockIdx.z;
+    const __nv_bfloat16 *xb = x + (int64_t)nb * nvox * xa.cstride + xa.coff;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmem_slot)), "r"(kTcCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid < kTcStages)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bars[tid])) : "memory");
+    if (tid == 0) gave_up = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    // A row of this thread: voxel v0 + tid; B row (threads 0-63): channel co0 + tid / 2, half tid & 1
+    const int64_t v = v0 + tid;
+    const bool vok = v < nvox;
+    const int z = vok ? (int)(v / ((int64_t)xa.h * xa.w)) : 0;
+    const int rem = vok ? (int)(v - (int64_t)z * xa.h * xa.w) : 0;
+    const int yy0 = rem / xa.w, xx0 = rem - (rem / xa.w) * xa.w;
+    const bool bload = tid < 2 * kTcN;
+    const int bn = tid >> 1, bh = tid & 1;
+    const bool bok = bload && co0 + bn < cout;
+    // canonical offsets: row r -> (r / 8) * 256 + (r % 8) * 16, K-half h -> + h * 128
+    const uint32_t aoff = (uint32_t)((tid >> 3) * 256 + (tid & 7) * 16);
+    const uint32_t boff = (uint32_t)((bn >> 3) * 256 + (bn & 7) * 16 + bh * 128);
+
+    uint4 ra0, ra1, rb;
+    auto load = [&](int tap, int c0) {
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+        const int zz = z + dz, yy = yy0 + dy, xx = xx0 + dx;
+        const bool in = vok && zz >= 0 && zz < xa.d && yy >= 0 && yy < xa.h && xx >= 0 && xx < xa.w;
+        ra0 = ra1 = make_uint4(0, 0, 0, 0);
+        if (in) {
+            const __nv_bfloat16 *p = xb + (((int64_t)zz * xa.h + yy) * xa.w + xx) * xa.cstride + c0;
+            ra0 = *reinterpret_cast<const uint4 *>(p);
+            ra1 = *reinterpret_cast<const uint4 *>(p + 8);
+        }
+        rb = make_uint4(0, 0, 0, 0);
+        if (bok) rb = *reinterpret_cast<const uint4 *>(wt + ((int64_t)(co0 + bn) * 27 + tap) * cin + c0 + 8 * bh);
+    };
+
+    const int nck = cin / kCK, steps = 27 * nck;
+    int tap = 0, ck = 0;
+    load(0, 0);
+    for (int s = 0; s < steps; ++s) {
+        const int st = s % kTcStages;
+        if (s >= kTcStages) {  // the MMA that read this stage kTcStages steps ago has completed
+            if (!mbar_wait(smem_u32(&bars[st]), (uint32_t)((s / kTcStages - 1) & 1))) {
+                gave_up = 1;  // benign race: every writer stores 1
+            }
+        }
+        __syncthreads();
+        if (gave_up) break;
+        *reinterpret_cast<uint4 *>(&sA[st][aoff]) = ra0;
+        *reinterpret_cast<uint4 *>(&sA[st][aoff + 128]) = ra1;
+        if (bload) *reinterpret_cast<uint4 *>(&sB[st][boff]) = rb;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        int ntap = tap, nc = ck + 1;
+        if (nc == nck) {
+            nc = 0;
+            ++ntap;
+        }
+        if (s + 1 < steps) load(ntap, nc * kCK);
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint64_t ad = tc_desc(smem_u32(sA[st]), 128, 256);
+            const uint64_t bd = tc_desc(smem_u32(sB[st]), 128, 256);
+            const uint32_t acc = s > 0 ? 1u : 0u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                :: "r"(tmem), "l"(ad), "l"(bd), "r"(kTcIdesc), "r"(acc) : "memory");
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         :: "r"(smem_u32(&bars[st])) : "memory");
+        }
+        tap = ntap;
+        ck = nc;
+    }
+    // the last commit covers every MMA issued before it
+    const int issued = gave_up ? 0 : steps;
+    bool ok = !gave_up;
+    if (issued > 0) {
+        const int last = issued - 1;
+        ok = mbar_wait(smem_u32(&bars[last % kTcStages]), (uint32_t)((last / kTcStages) & 1)) && ok;
+    } else if (tid == 0) {
+        // a timeout left MMAs in flight: wait (bounded) on every stage's pending phase
+        for (int st = 0; st < kTcStages; ++st) mbar_wait(smem_u32(&bars[st]), 0);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        uint32_t r[32];
+        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (vok) {
+            const int64_t o = ((int64_t)nb * nvox + v) * ya.cstride + ya.coff + co0;
+#pragma unroll
+            for (int j = 0; j < kTcN; j += 8) {
+                if (co0 + j >= cout) break;
+                float f[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    float t = __uint_as_float(r[j + e]) + (bias ? bias[co0 + j + e] : 0.0f);
+                    f[e] = relu ? fmaxf(t, 0.0f) : t;
+                }
+                __nv_bfloat162 h[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) h[e] = __floats2bfloat162_rn(f[2 * e], f[2 * e + 1]);
+                *reinterpret_cast<uint4 *>(y + o + j) = *reinterpret_cast<const uint4 *>(h);
+                if (yf) {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) yf[o + j + e] = f[e];
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(&g_tc_status, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTcCols) : "memory");
+}
+
+static int g_conv_tc = 0;  // srf_set_conv_tc: 1 = the tcgen05 kernel for 128 x 32 tiles
+
 // Small grids (too few CTAs to hide the latency of a long chain of K steps): each of the 4 warps
 // walks every 4th (tap, 16-channel) step of the whole 64-voxel x 32-channel tile through its own
 // double buffer, synchronising only within the warp; the four partial tiles are then summed
@@ -739,12 +936,29 @@ int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *
         k_conv3d_fwd<64, 64><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
     } else if (ctas(128, 32) >= fill) {
         dim3 grid((unsigned)((nvox + 127) / 128), (unsigned)((cout + 31) / 32), (unsigned)xa.n);
-        k_conv3d_fwd<128, 32><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
+        if (g_conv_tc && cout % 32 == 0 && ya.cstride % 8 == 0 && ya.coff % 8 == 0 && (uintptr_t)y % 16 == 0)
+            k_conv3d_fwd_tc<<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
+        else
+            k_conv3d_fwd<128, 32><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
     } else {  // too few CTAs to hide a long K chain: split K over the warps of each CTA
         dim3 grid((unsigned)((nvox + kWsM - 1) / kWsM), (unsigned)((cout + kWsN - 1) / kWsN), (unsigned)xa.n);
         k_conv3d_fwd_wsplit<<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
     }
     return check_cuda("conv3d forward launch");
+}
+
+int srf_set_conv_tc(int32_t on) {
+    g_conv_tc = on ? 1 : 0;
+    return ok();
+}
+
+int srf_conv_tc_status(int32_t *status) {
+    if (!status) return fail(SRF_EINVAL, "NULL argument");
+    int h = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&h, g_tc_status, sizeof(int));
+    if (e != cudaSuccess) return check_cuda("conv tc status");
+    *status = h;
+    return ok();
 }
 
 int srf_conv3d_wgrad(const void *x, const int32_t xs[6], int32_t cin, const void *dy, const int32_t ds[6],

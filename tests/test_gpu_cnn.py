@@ -4,6 +4,8 @@ Inputs and weights are drawn as bfloat16 values, so the oracle sees exactly what
 see; the FP32-accumulated results must match to 1e-5 relative, BF16-stored results to BF16
 rounding (4e-3).
 """
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -85,6 +87,43 @@ def test_conv_forward_tile_shapes(cuda_lib, cnn):
         ref = cnn.conv3d(_np(x), _np(wt), bias.cpu().numpy(), relu=True)
         assert rel_l2(yf.cpu().numpy(), ref) <= 1e-5, (shape, cin, cout)
         assert rel_l2(_np(y), ref) <= 4e-3
+
+
+def test_conv_forward_tcgen05_tile(cuda_lib, cnn):
+    """The 128-voxel x 32-channel tile on tcgen05.mma (accumulator in tensor memory) against the
+    oracle and against the mma.sync kernel: input and output channel slices of wider buffers,
+    Cin 16 / 96 / 32, Cout 32 / 32 / 96, a grid whose last tile is partial."""
+    from srf_gb300._lib import call, i32, ptr, stream_ptr
+    from srf_gb300.surrogate import act
+    rng = np.random.default_rng(9)
+    dev = torch.device("cuda", 0)
+    s = stream_ptr(dev)
+    cases = (((1, 25, 40, 40), 16, 32, 0, 0), ((1, 25, 40, 40), 96, 32, 16, 32), ((1, 25, 40, 41), 32, 96, 0, 32))
+    try:
+        for shape, cin, cout, xoff, yoff in cases:
+            xbuf = _bf(rng.standard_normal(shape + (cin + xoff,))).to(dev)
+            wt = _bf(rng.standard_normal((cout, 27, cin)) * 0.1).to(dev)
+            bias = torch.as_tensor(rng.standard_normal(cout).astype(np.float32)).to(dev)
+            outs = []
+            for tc in (0, 1):
+                call("srf_set_conv_tc", i32(tc))
+                y = torch.zeros(shape + (cout + yoff,), dtype=torch.bfloat16, device=dev)
+                yf = torch.zeros(shape + (cout + yoff,), dtype=torch.float32, device=dev)
+                call("srf_conv3d_fwd", ptr(xbuf), act(xbuf, xoff), i32(cin), ptr(wt), ptr(bias), i32(cout),
+                     i32(1), ptr(y), act(y, yoff), ptr(yf), s)
+                outs.append((y, yf))
+            status = ctypes.c_int32(0)
+            call("srf_conv_tc_status", ctypes.byref(status))
+            assert status.value == 0
+            ref = cnn.conv3d(_np(xbuf)[..., xoff:], _np(wt), bias.cpu().numpy(), relu=True)
+            (y0, f0), (y1, f1) = outs
+            got = f1.cpu().numpy()[..., yoff:]
+            assert rel_l2(got, ref) <= 1e-5, (shape, cin, cout)
+            assert rel_l2(f1.cpu().numpy()[..., yoff:], f0.cpu().numpy()[..., yoff:]) <= 1e-6
+            assert rel_l2(_np(y1)[..., yoff:], ref) <= 4e-3
+            assert np.all(_np(y1)[..., :yoff] == 0)
+    finally:
+        call("srf_set_conv_tc", i32(0))
 
 
 def test_pool_upsample_and_adjoints(cuda_lib, cnn):
