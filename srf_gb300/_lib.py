@@ -30,7 +30,7 @@ EXPORTS = (
     "srf_osem_update_batch", "srf_emap_block_full", "srf_sss",
     "srf_backprojection_tof_noalloc", "srf_listmode_snap", "srf_lm2sino", "srf_attenuation",
     "srf_conv3d_fwd", "srf_conv3d_wgrad", "srf_conv3d_flip_weights", "srf_cnn_relu_bwd",
-    "srf_set_conv_tc", "srf_conv_tc_status",
+    "srf_set_conv_tc", "srf_conv_tc_status", "srf_conv_last_path",
     "srf_cnn_bias_grad", "srf_cnn_pool2", "srf_cnn_upsample2", "srf_cnn_add", "srf_cnn_head8", "srf_calib_l2", "srf_calib_sink_size",
     "srf_cnn_rel_mse", "srf_cnn_adam", "srf_spot_fit", "srf_scale_by_basis",
     "srf_deform", "srf_shift", "srf_shift_z", "srf_rotate", "srf_deform_invert",

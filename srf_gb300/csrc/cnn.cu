@@ -17,6 +17,7 @@
 // accumulated with FP32 atomics. Requirements (checked on the host): Cin and Cout multiples of
 // 16, channel strides and offsets multiples of 8 (16-byte aligned rows).
 #include <algorithm>
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -387,7 +388,267 @@ k_conv3d_fwd_tc(const __nv_bfloat16 *__restrict__ x, Act xa, int cin, const __nv
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTcCols) : "memory");
 }
 
-static int g_conv_tc = 0;  // srf_set_conv_tc: 1 = the tcgen05 kernel for 128 x 32 tiles
+static int g_conv_tc = 1;    // srf_set_conv_tc: 0 mma.sync only, 1 tcgen05 K-step tiles, 2 also TMA halo tiles
+static int g_conv_path = -1;  // kernel of the last srf_conv3d_fwd launch (srf_conv_last_path)
+
+// ---------------------------------------------------------------- tcgen05 + TMA, halo tiles
+// Batch-1 layers on wide grids (W >= 96, Cout = 32): an output tile is 128 consecutive voxels of
+// one x-row. Its input halo (rows x0 - 1 .. x0 + 128 of the 3 x 3 (z, y) neighbour rows, 16
+// channels per group) is one TMA box per 8-channel chunk, written by the TMA unit in the
+// canonical no-swizzle K-major layout [chunk][z][y][x][8 channels] (rows 16 B apart, zero fill
+// outside the volume = the convolution's padding). Every tap's A operand is then the same halo
+// at a row offset: descriptor start = halo + ((dz + 1) * 3 + dy + 1) * 130 rows + dx + 1, so the
+// 27 taps of a 16-channel group are 27 back-to-back tcgen05.mma with no gather and no barrier
+// between them. The weights of the group (B, [chunk][tap][co][8]) are staged with cp.async by all
+// threads. Persistent CTAs (one per SM) walk (tile, group) items through two stages: the next
+// item's TMA and cp.async copies are in flight while the tensor cores work on the current one;
+// a stage is refilled when the mbarrier its MMAs committed to has fired. The accumulator lives
+// in 32 TMEM columns; after a tile's last group it is read with tcgen05.ld for the bias and
+// activation epilogue. Bounded waits as in k_conv3d_fwd_tc. Measured slower than the K-step
+// kernels on the surrogate's level-1 layers (62 against 33-43 us at Cin 16): a TMA box whose
+// inner extent is one 16-byte channel chunk moves 2,340 separate rows per halo. Mode 2 only.
+constexpr int kHx = 130;                               // halo rows along x
+constexpr int kHPlane = 9 * kHx * 16;                  // one 8-channel chunk of the halo: 18,720 B
+constexpr int kHPlanePad = (kHPlane + 127) / 128 * 128;  // TMA destinations are 128-byte aligned
+constexpr int kHABytes = 2 * kHPlanePad;               // a 16-channel group
+constexpr int kHBBytes = 2 * 27 * kTcN * 16;           // [chunk][tap][co][16 B] = 27,648 B
+constexpr int kHStage = kHABytes + kHBBytes;
+constexpr int kHMaxChunks = 16;                        // Cin <= 128
+constexpr int kHSmem = 2 * kHStage + 1024;             // two stages + alignment slack
+
+struct HaloMaps {
+    CUtensorMap m[kHMaxChunks];  // chunk c: dims (8 channels, W, H, D) from channel 8c of the slice
+};
+
+__global__ void __launch_bounds__(128, 1)
+k_conv3d_fwd_halo(const __grid_constant__ HaloMaps maps, Act xa, int cin, const __nv_bfloat16 *__restrict__ wt,
+                  const float *__restrict__ bias, int relu, __nv_bfloat16 *__restrict__ y, Act ya,
+                  float *__restrict__ yf) {
+    extern __shared__ unsigned char dsm[];
+    __shared__ __align__(8) uint64_t full[2], empty[2], done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int gave_up;
+    unsigned char *base = (unsigned char *)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int G = cin / 16;
+    const int tx = (xa.w + kTcM - 1) / kTcM;
+    const int64_t n_tiles = (int64_t)xa.d * xa.h * tx;
+    const int64_t my_tiles = n_tiles > blockIdx.x ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t items = my_tiles * G;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmem_slot)), "r"(kTcCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid < 2) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&full[tid])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&empty[tid])) : "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&done)) : "memory");
+        gave_up = 0;
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    auto tile_of = [&](int64_t it, int &z, int &yy, int &x0) {
+        const int64_t t = blockIdx.x + (it / G) * (int64_t)gridDim.x;
+        const int xt = (int)(t % tx);
+        const int64_t zy = t / tx;
+        yy = (int)(zy % xa.h);
+        z = (int)(zy / xa.h);
+        x0 = xt * kTcM;
+    };
+    // copies of item `it` into stage st: TMA of the two halo chunks (thread 0), weights (all)
+    auto issue = [&](int64_t it, int st) {
+        int z, yy, x0;
+        tile_of(it, z, yy, x0);
+        const int g = (int)(it % G);
+        unsigned char *sa = base + st * kHStage, *sb = sa + kHABytes;
+        const uint32_t fb = smem_u32(&full[st]);
+        if (tid == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                         :: "r"(fb), "r"((uint32_t)(2 * kHPlane)) : "memory");
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const uint64_t map = reinterpret_cast<uint64_t>(&maps.m[2 * g + c]);
+                asm volatile(
+                    "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                    " [%0], [%1, {%2, %3, %4, %5}], [%6];"
+                    :: "r"(smem_u32(sa + c * kHPlanePad)), "l"(map), "r"(0), "r"(x0 - 1), "r"(yy - 1), "r"(z - 1),
+                       "r"(fb) : "memory");
+            }
+        }
+        for (int j = tid; j < 2 * 27 * kTcN; j += blockDim.x) {  // j = (chunk * 27 + tap) * 32 + co
+            const int co = j & (kTcN - 1), tap = (j >> 5) % 27, c = (j >> 5) / 27;
+            const __nv_bfloat16 *src = wt + ((int64_t)co * 27 + tap) * cin + 16 * g + 8 * c;
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(smem_u32(sb + j * 16)), "l"(src) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+
+    if (items > 0) issue(0, 0);
+    int tiles_done = 0;
+    for (int64_t it = 0; it < items; ++it) {
+        const int st = (int)(it & 1);
+        const int g = (int)(it % G);
+        if (it + 1 < items) {
+            if (it >= 1 && !mbar_wait(smem_u32(&empty[st ^ 1]), (uint32_t)(((it - 1) >> 1) & 1))) gave_up = 1;
+            else issue(it + 1, st ^ 1);
+        } else {
+            asm volatile("cp.async.commit_group;" ::: "memory");
+        }
+        asm volatile("cp.async.wait_group 1;" ::: "memory");  // item it's weights have landed
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (gave_up) break;
+        if (tid == 0) {
+            if (!mbar_wait(smem_u32(&full[st]), (uint32_t)((it >> 1) & 1))) {
+                gave_up = 1;
+            } else {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t sa = smem_u32(base + st * kHStage), sb = sa + kHABytes;
+                for (int tap = 0; tap < 27; ++tap) {
+                    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;  // halo row offsets
+                    const uint64_t ad = tc_desc(sa + (uint32_t)(((dz * 3 + dy) * kHx + dx) * 16), kHPlanePad, 128);
+                    const uint64_t bd = tc_desc(sb + (uint32_t)(tap * kTcN * 16), 27 * kTcN * 16, 128);
+                    const uint32_t acc = (g == 0 && tap == 0) ? 0u : 1u;
+                    asm volatile(
+                        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                        :: "r"(tmem), "l"(ad), "l"(bd), "r"(kTcIdesc), "r"(acc) : "memory");
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                             :: "r"(smem_u32(&empty[st])) : "memory");
+                if (g == G - 1)
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                                 :: "r"(smem_u32(&done)) : "memory");
+            }
+        }
+        __syncthreads();
+        if (gave_up) break;
+        if (g == G - 1) {  // the tile's accumulator is complete: epilogue
+            int z, yy, x0;
+            tile_of(it, z, yy, x0);
+            const bool ok = mbar_wait(smem_u32(&done), (uint32_t)(tiles_done & 1));
+            ++tiles_done;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (!ok) {
+                gave_up = 1;
+            } else {
+                uint32_t r[32];
+                const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+                      "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+                      "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                const int x = x0 + tid;
+                if (x < xa.w) {
+                    const int64_t o = (((int64_t)z * xa.h + yy) * xa.w + x) * ya.cstride + ya.coff;
+#pragma unroll
+                    for (int j = 0; j < kTcN; j += 8) {
+                        float f[8];
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            const float t = __uint_as_float(r[j + e]) + (bias ? bias[j + e] : 0.0f);
+                            f[e] = relu ? fmaxf(t, 0.0f) : t;
+                        }
+                        __nv_bfloat162 h[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) h[e] = __floats2bfloat162_rn(f[2 * e], f[2 * e + 1]);
+                        *reinterpret_cast<uint4 *>(y + o + j) = *reinterpret_cast<const uint4 *>(h);
+                        if (yf) {
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) yf[o + j + e] = f[e];
+                        }
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();  // the next tile's first MMA overwrites the accumulator
+            if (gave_up) break;
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    if (gave_up) {
+        if (tid == 0) {
+            atomicExch(&g_tc_status, 1);
+            // bounded waits for copies and MMAs that may still be in flight
+            mbar_wait(smem_u32(&full[0]), 0);
+            mbar_wait(smem_u32(&full[1]), 0);
+            mbar_wait(smem_u32(&empty[0]), 0);
+            mbar_wait(smem_u32(&empty[1]), 0);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTcCols) : "memory");
+}
+
+// cuTensorMapEncodeTiled from the driver (the runtime is linked statically; no -lcuda)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+// Launches the halo kernel when the layer qualifies and its tensor maps encode; false otherwise
+// (the caller then takes another kernel).
+static bool launch_halo(const __nv_bfloat16 *x, const Act &xa, int cin, const __nv_bfloat16 *w, const float *bias,
+                        int cout, int relu, __nv_bfloat16 *y, const Act &ya, float *yf, cudaStream_t s) {
+    if (xa.n != 1 || cout != kTcN || cin % 16 || cin / 8 > kHMaxChunks || xa.w < 96) return false;
+    if (xa.cstride % 8 || xa.coff % 8 || ya.cstride % 8 || ya.coff % 8) return false;
+    if ((uintptr_t)x % 16 || (uintptr_t)w % 16 || (uintptr_t)y % 16) return false;
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return false;
+    HaloMaps maps;
+    const cuuint64_t dims[4] = {8, (cuuint64_t)xa.w, (cuuint64_t)xa.h, (cuuint64_t)xa.d};
+    const cuuint64_t row = (cuuint64_t)xa.cstride * 2;
+    const cuuint64_t strides[3] = {row, row * xa.w, row * xa.w * xa.h};
+    const cuuint32_t box[4] = {8, (cuuint32_t)kHx, 3, 3};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    for (int c = 0; c < cin / 8; ++c) {
+        void *addr = (void *)(x + xa.coff + 8 * c);
+        if (enc(&maps.m[c], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, addr, dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_conv3d_fwd_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, kHSmem) != cudaSuccess)
+            return false;
+        attr = true;
+    }
+    const int64_t n_tiles = (int64_t)xa.d * xa.h * ((xa.w + kTcM - 1) / kTcM);
+    const unsigned grid = (unsigned)std::min<int64_t>(n_tiles, num_sms());
+    k_conv3d_fwd_halo<<<grid, 128, kHSmem, s>>>(maps, xa, cin, w, bias, relu, y, ya, yf);
+    return true;
+}
+
+
 
 // Small grids (too few CTAs to hide the latency of a long chain of K steps): each of the 4 warps
 // walks every 4th (tap, 16-channel) step of the whole 64-voxel x 32-channel tile through its own
@@ -934,21 +1195,36 @@ int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *
     if (cout % 64 == 0 && ctas(64, 64) >= fill) {
         dim3 grid((unsigned)((nvox + 63) / 64), (unsigned)(cout / 64), (unsigned)xa.n);
         k_conv3d_fwd<64, 64><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
+        g_conv_path = 0;
+    } else if (g_conv_tc >= 2 && launch_halo(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf, s)) {
+        g_conv_path = 3;  // batch-1 wide layers: tcgen05 on TMA-loaded halo tiles
     } else if (ctas(128, 32) >= fill) {
         dim3 grid((unsigned)((nvox + 127) / 128), (unsigned)((cout + 31) / 32), (unsigned)xa.n);
-        if (g_conv_tc && cout % 32 == 0 && ya.cstride % 8 == 0 && ya.coff % 8 == 0 && (uintptr_t)y % 16 == 0)
+        if (g_conv_tc && cout % 32 == 0 && ya.cstride % 8 == 0 && ya.coff % 8 == 0 && (uintptr_t)y % 16 == 0 &&
+            (uintptr_t)x % 16 == 0 && (uintptr_t)w % 16 == 0) {
             k_conv3d_fwd_tc<<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
-        else
+            g_conv_path = 2;
+        } else {
             k_conv3d_fwd<128, 32><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
+            g_conv_path = 1;
+        }
     } else {  // too few CTAs to hide a long K chain: split K over the warps of each CTA
         dim3 grid((unsigned)((nvox + kWsM - 1) / kWsM), (unsigned)((cout + kWsN - 1) / kWsN), (unsigned)xa.n);
         k_conv3d_fwd_wsplit<<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
+        g_conv_path = 4;
     }
     return check_cuda("conv3d forward launch");
 }
 
-int srf_set_conv_tc(int32_t on) {
-    g_conv_tc = on ? 1 : 0;
+int srf_set_conv_tc(int32_t mode) {
+    if (mode < 0 || mode > 2) return fail(SRF_EINVAL, "conv mode must be 0, 1 or 2");
+    g_conv_tc = mode;
+    return ok();
+}
+
+int srf_conv_last_path(int32_t *path) {
+    if (!path) return fail(SRF_EINVAL, "NULL argument");
+    *path = g_conv_path;
     return ok();
 }
 
