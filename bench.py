@@ -57,13 +57,14 @@ def parse():
     ap.add_argument("--seed", type=int, default=20250101)
     ap.add_argument("--workload", default="clinical",
                     choices=["clinical", "batched", "components", "surrogate", "profile", "autograd",
-                             "mlem_small"],
+                             "mlem_small", "conv"],
                     help="clinical: the TOF OSEM headline; batched: 64 uneven studies; "
                          "components: every kernel of the path against the CPU oracle; "
                          "surrogate: learned scatter estimate against SSS (time, sinogram and "
                          "OSEM image agreement); profile: subset steps only, the case ncu captures; "
                          "autograd: differentiable projector, 8 images, forward + backward; "
-                         "mlem_small: non-TOF MLEM, 1e5 events, 640-crystal scanner, 64x64x16")
+                         "mlem_small: non-TOF MLEM, 1e5 events, 640-crystal scanner, 64x64x16; "
+                         "conv: the surrogate's full-resolution 3-D convolutions in each kernel mode")
     ap.add_argument("--held-out", type=int, default=20, help="surrogate: held-out phantoms timed")
     ap.add_argument("--studies", type=int, default=64)
     ap.add_argument("--autotune", action="store_true", help="tune lanes/slabs per lane first")
@@ -416,6 +417,66 @@ def run_batched(a, ws, rank, local):
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)
+
+
+def run_conv(a, ws, rank, local):
+    """The scatter U-Net's full-resolution convolutions (batch 1, 28 x 28 x 160 voxels, Cin 16 / 32 /
+    96 -> Cout 32, BF16 with FP32 accumulation) in each srf_conv3d_fwd kernel mode: 0 mma.sync,
+    1 tcgen05 K-step tiles (the default), 2 / 3 tcgen05 on halo tiles loaded by cp.async / TMA. CUDA events, best of
+    --steps after --warmup; the kernel each mode took is reported (srf_conv_last_path)."""
+    import ctypes
+    import numpy as np
+    import torch
+    from srf_gb300 import _lib
+    from srf_gb300._lib import call, i32, ptr, stream_ptr
+    from srf_gb300.surrogate import act
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.load()
+    s = stream_ptr(dev)
+    rng = np.random.default_rng(a.seed)
+    shape = (1, 28, 28, 160)
+    names = {0: "mma.sync 64x64", 1: "mma.sync 128x32", 2: "tcgen05 K-step", 3: "tcgen05 TMA halo",
+             4: "mma.sync split-K", 5: "tcgen05 cp.async halo"}
+    layers = []
+    try:
+        for cin, cout in ((16, 32), (32, 32), (96, 32)):
+            x = torch.as_tensor(rng.standard_normal(shape + (cin,)).astype(np.float32)).to(torch.bfloat16).to(dev)
+            w = (torch.as_tensor(rng.standard_normal((cout, 27, cin)).astype(np.float32)) * 0.1).to(torch.bfloat16).to(dev)
+            b = torch.zeros(cout, device=dev)
+            y = torch.empty(shape + (cout,), dtype=torch.bfloat16, device=dev)
+            flops = 2.0 * 27 * cin * cout * float(np.prod(shape))
+            rec = {"cin": cin, "cout": cout, "gflop": flops / 1e9}
+            for mode in (0, 1, 2, 3):
+                call("srf_set_conv_tc", i32(mode))
+                run = lambda: call("srf_conv3d_fwd", ptr(x), act(x), i32(cin), ptr(w), ptr(b), i32(cout), i32(1),
+                                   ptr(y), act(y), None, s)
+                for _ in range(max(a.warmup, 1)):
+                    run()
+                torch.cuda.synchronize()
+                best = float("inf")
+                for _ in range(a.steps):
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    run()
+                    e1.record()
+                    torch.cuda.synchronize()
+                    best = min(best, e0.elapsed_time(e1))
+                path = ctypes.c_int32(-1)
+                call("srf_conv_last_path", ctypes.byref(path))
+                rec[f"mode{mode}"] = {"us": 1000 * best, "tflops": flops / (best * 1e-3) / 1e12,
+                                      "kernel": names.get(path.value, str(path.value))}
+            layers.append(rec)
+    finally:
+        call("srf_set_conv_tc", i32(1))
+    if rank == 0:
+        tot = {m: sum(l[f"mode{m}"]["us"] for l in layers) for m in (0, 1, 2, 3)}
+        print(json.dumps({
+            "metric": "full-resolution 3-D convolution time of the scatter U-Net (three layers)",
+            "value": tot[1], "unit": "us", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (fp32 accumulation)",
+            "data": "synthetic (seeded)", "config": {"workload": "conv", "grid": list(shape[1:]), "batch": 1},
+            "layers": layers, "total_us_by_mode": tot, "gpu_launches": 12 * (a.steps + max(a.warmup, 1))}), flush=True)
 
 
 def run_mlem_small(a, ws, rank, local):
@@ -866,6 +927,9 @@ def main():
         return
     if a.workload == "mlem_small":
         run_mlem_small(a, ws, rank, local)
+        return
+    if a.workload == "conv":
+        run_conv(a, ws, rank, local)
         return
     run_clinical(a, ws, rank, local)
     if ws > 1:

@@ -332,15 +332,15 @@ int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *
                    int32_t cout, int32_t relu, void *y, const int32_t ys[6], float *yf, void *stream);
 /* Kernels of srf_conv3d_fwd, process-wide, read at launch. mode 1 (the default): its
  * 128-voxel x 32-channel tiles run on tcgen05.mma with the accumulator in tensor memory; 2: in
- * addition, batch-1 layers with W >= 96 and Cout = 32 on the TMA halo-tile kernel; 0: mma.sync
- * only. */
+ * addition, batch-1 layers with W >= 96 and Cout = 32 on the halo-tile tcgen05 kernel, halos
+ * loaded by the threads (cp.async); 3: the same with the halos loaded by TMA; 0: mma.sync only. */
 int srf_set_conv_tc(int32_t mode);
 /* *status = 1 if a tcgen05 convolution gave up waiting for its tensor-core work (bounded waits),
  * else 0. Synchronises with the device. */
 int srf_conv_tc_status(int32_t *status);
 /* *path = the kernel of the last srf_conv3d_fwd launch: 0 mma.sync 64 x 64, 1 mma.sync 128 x 32,
- * 2 tcgen05 128 x 32 (gathered K steps), 3 tcgen05 on TMA halo tiles (batch 1, W >= 96,
- * Cout = 32), 4 mma.sync split-K; -1 before the first. */
+ * 2 tcgen05 128 x 32 (gathered K steps), 3 tcgen05 on TMA halo tiles, 4 mma.sync split-K,
+ * 5 tcgen05 on cp.async halo tiles; -1 before the first. */
 int srf_conv_last_path(int32_t *path);
 /* dw[co][tap][ci] += sum_v dy[v, co] x[v + tap - 1, ci] (FP32 accumulation). */
 int srf_conv3d_wgrad(const void *x, const int32_t xs[6], int32_t cin, const void *dy, const int32_t ds[6],

@@ -17,6 +17,7 @@
 // accumulated with FP32 atomics. Requirements (checked on the host): Cin and Cout multiples of
 // 16, channel strides and offsets multiples of 8 (16-byte aligned rows).
 #include <algorithm>
+#include <cstring>
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -388,7 +389,7 @@ k_conv3d_fwd_tc(const __nv_bfloat16 *__restrict__ x, Act xa, int cin, const __nv
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTcCols) : "memory");
 }
 
-static int g_conv_tc = 1;    // srf_set_conv_tc: 0 mma.sync only, 1 tcgen05 K-step tiles, 2 also TMA halo tiles
+static int g_conv_tc = 1;    // srf_set_conv_tc: 0 mma.sync, 1 tcgen05 K-step tiles, 2/3 also halo tiles (cp.async / TMA)
 static int g_conv_path = -1;  // kernel of the last srf_conv3d_fwd launch (srf_conv_last_path)
 
 // ---------------------------------------------------------------- tcgen05 + TMA, halo tiles
@@ -396,7 +397,8 @@ static int g_conv_path = -1;  // kernel of the last srf_conv3d_fwd launch (srf_c
 // one x-row. Its input halo (rows x0 - 1 .. x0 + 128 of the 3 x 3 (z, y) neighbour rows, 16
 // channels per group) is one TMA box per 8-channel chunk, written by the TMA unit in the
 // canonical no-swizzle K-major layout [chunk][z][y][x][8 channels] (rows 16 B apart, zero fill
-// outside the volume = the convolution's padding). Every tap's A operand is then the same halo
+// outside the volume = the convolution's padding; TMA = false: the same layout written by the
+// threads with zero-filling cp.async). Every tap's A operand is then the same halo
 // at a row offset: descriptor start = halo + ((dz + 1) * 3 + dy + 1) * 130 rows + dx + 1, so the
 // 27 taps of a 16-channel group are 27 back-to-back tcgen05.mma with no gather and no barrier
 // between them. The weights of the group (B, [chunk][tap][co][8]) are staged with cp.async by all
@@ -404,9 +406,9 @@ static int g_conv_path = -1;  // kernel of the last srf_conv3d_fwd launch (srf_c
 // item's TMA and cp.async copies are in flight while the tensor cores work on the current one;
 // a stage is refilled when the mbarrier its MMAs committed to has fired. The accumulator lives
 // in 32 TMEM columns; after a tile's last group it is read with tcgen05.ld for the bias and
-// activation epilogue. Bounded waits as in k_conv3d_fwd_tc. Measured slower than the K-step
-// kernels on the surrogate's level-1 layers (62 against 33-43 us at Cin 16): a TMA box whose
-// inner extent is one 16-byte channel chunk moves 2,340 separate rows per halo. Mode 2 only.
+// activation epilogue. Bounded waits as in k_conv3d_fwd_tc. The TMA form measured slower than
+// the K-step kernels on the surrogate's level-1 layers (62 against 33-43 us at Cin 16): a TMA
+// box whose inner extent is one 16-byte channel chunk moves 2,340 separate rows per halo.
 constexpr int kHx = 130;                               // halo rows along x
 constexpr int kHPlane = 9 * kHx * 16;                  // one 8-channel chunk of the halo: 18,720 B
 constexpr int kHPlanePad = (kHPlane + 127) / 128 * 128;  // TMA destinations are 128-byte aligned
@@ -420,10 +422,11 @@ struct HaloMaps {
     CUtensorMap m[kHMaxChunks];  // chunk c: dims (8 channels, W, H, D) from channel 8c of the slice
 };
 
-__global__ void __launch_bounds__(128, 1)
-k_conv3d_fwd_halo(const __grid_constant__ HaloMaps maps, Act xa, int cin, const __nv_bfloat16 *__restrict__ wt,
-                  const float *__restrict__ bias, int relu, __nv_bfloat16 *__restrict__ y, Act ya,
-                  float *__restrict__ yf) {
+template <bool TMA>
+__global__ void __launch_bounds__(256, 1)
+k_conv3d_fwd_halo(const __grid_constant__ HaloMaps maps, const __nv_bfloat16 *__restrict__ x, Act xa, int cin,
+                  const __nv_bfloat16 *__restrict__ wt, const float *__restrict__ bias, int relu,
+                  __nv_bfloat16 *__restrict__ y, Act ya, float *__restrict__ yf) {
     extern __shared__ unsigned char dsm[];
     __shared__ __align__(8) uint64_t full[2], empty[2], done;
     __shared__ uint32_t tmem_slot;
@@ -470,7 +473,7 @@ k_conv3d_fwd_halo(const __grid_constant__ HaloMaps maps, Act xa, int cin, const 
         const int g = (int)(it % G);
         unsigned char *sa = base + st * kHStage, *sb = sa + kHABytes;
         const uint32_t fb = smem_u32(&full[st]);
-        if (tid == 0) {
+        if (TMA && tid == 0) {
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
                          :: "r"(fb), "r"((uint32_t)(2 * kHPlane)) : "memory");
 #pragma unroll
@@ -483,10 +486,21 @@ k_conv3d_fwd_halo(const __grid_constant__ HaloMaps maps, Act xa, int cin, const 
                        "r"(fb) : "memory");
             }
         }
+        if (!TMA) {  // the halo rows by the threads, zero outside the volume
+            const __nv_bfloat16 *xg = x + xa.coff + 16 * g;
+            for (int j = tid; j < 2 * 9 * kHx; j += blockDim.x) {  // j = chunk * 1170 + row
+                const int c = j / (9 * kHx), r = j - c * (9 * kHx);
+                const int gz = z - 1 + r / (3 * kHx), gy = yy - 1 + (r / kHx) % 3, gx = x0 - 1 + r % kHx;
+                const bool in = gz >= 0 && gz < xa.d && gy >= 0 && gy < xa.h && gx >= 0 && gx < xa.w;
+                const __nv_bfloat16 *src = in ? xg + (((int64_t)gz * xa.h + gy) * xa.w + gx) * xa.cstride + 8 * c : x;
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;"
+                             :: "r"(smem_u32(sa + c * kHPlanePad + r * 16)), "l"(src), "r"(in ? 16u : 0u) : "memory");
+            }
+        }
         for (int j = tid; j < 2 * 27 * kTcN; j += blockDim.x) {  // j = (chunk * 27 + tap) * 32 + co
             const int co = j & (kTcN - 1), tap = (j >> 5) % 27, c = (j >> 5) / 27;
             const __nv_bfloat16 *src = wt + ((int64_t)co * 27 + tap) * cin + 16 * g + 8 * c;
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(smem_u32(sb + j * 16)), "l"(src) : "memory");
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" :: "r"(smem_u32(sb + j * 16)), "l"(src) : "memory");
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
@@ -507,7 +521,7 @@ k_conv3d_fwd_halo(const __grid_constant__ HaloMaps maps, Act xa, int cin, const 
         __syncthreads();
         if (gave_up) break;
         if (tid == 0) {
-            if (!mbar_wait(smem_u32(&full[st]), (uint32_t)((it >> 1) & 1))) {
+            if (TMA && !mbar_wait(smem_u32(&full[st]), (uint32_t)((it >> 1) & 1))) {
                 gave_up = 1;
             } else {
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -539,7 +553,7 @@ k_conv3d_fwd_halo(const __grid_constant__ HaloMaps maps, Act xa, int cin, const 
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (!ok) {
                 gave_up = 1;
-            } else {
+            } else if (warp < 4) {  // warps 0-3 hold TMEM lanes 0-127, one output voxel per thread
                 uint32_t r[32];
                 const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
                 asm volatile(
@@ -583,8 +597,10 @@ k_conv3d_fwd_halo(const __grid_constant__ HaloMaps maps, Act xa, int cin, const 
         if (tid == 0) {
             atomicExch(&g_tc_status, 1);
             // bounded waits for copies and MMAs that may still be in flight
-            mbar_wait(smem_u32(&full[0]), 0);
-            mbar_wait(smem_u32(&full[1]), 0);
+            if (TMA) {
+                mbar_wait(smem_u32(&full[0]), 0);
+                mbar_wait(smem_u32(&full[1]), 0);
+            }
             mbar_wait(smem_u32(&empty[0]), 0);
             mbar_wait(smem_u32(&empty[1]), 0);
         }
@@ -617,34 +633,38 @@ static EncodeTiledFn encode_tiled() {
 // Launches the halo kernel when the layer qualifies and its tensor maps encode; false otherwise
 // (the caller then takes another kernel).
 static bool launch_halo(const __nv_bfloat16 *x, const Act &xa, int cin, const __nv_bfloat16 *w, const float *bias,
-                        int cout, int relu, __nv_bfloat16 *y, const Act &ya, float *yf, cudaStream_t s) {
+                        int cout, int relu, __nv_bfloat16 *y, const Act &ya, float *yf, bool tma, cudaStream_t s) {
     if (xa.n != 1 || cout != kTcN || cin % 16 || cin / 8 > kHMaxChunks || xa.w < 96) return false;
     if (xa.cstride % 8 || xa.coff % 8 || ya.cstride % 8 || ya.coff % 8) return false;
     if ((uintptr_t)x % 16 || (uintptr_t)w % 16 || (uintptr_t)y % 16) return false;
-    EncodeTiledFn enc = encode_tiled();
-    if (!enc) return false;
     HaloMaps maps;
-    const cuuint64_t dims[4] = {8, (cuuint64_t)xa.w, (cuuint64_t)xa.h, (cuuint64_t)xa.d};
-    const cuuint64_t row = (cuuint64_t)xa.cstride * 2;
-    const cuuint64_t strides[3] = {row, row * xa.w, row * xa.w * xa.h};
-    const cuuint32_t box[4] = {8, (cuuint32_t)kHx, 3, 3};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    for (int c = 0; c < cin / 8; ++c) {
-        void *addr = (void *)(x + xa.coff + 8 * c);
-        if (enc(&maps.m[c], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, addr, dims, strides, box, estr,
-                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return false;
+    memset(&maps, 0, sizeof(maps));
+    if (tma) {
+        EncodeTiledFn enc = encode_tiled();
+        if (!enc) return false;
+        const cuuint64_t dims[4] = {8, (cuuint64_t)xa.w, (cuuint64_t)xa.h, (cuuint64_t)xa.d};
+        const cuuint64_t row = (cuuint64_t)xa.cstride * 2;
+        const cuuint64_t strides[3] = {row, row * xa.w, row * xa.w * xa.h};
+        const cuuint32_t box[4] = {8, (cuuint32_t)kHx, 3, 3};
+        const cuuint32_t estr[4] = {1, 1, 1, 1};
+        for (int c = 0; c < cin / 8; ++c) {
+            void *addr = (void *)(x + xa.coff + 8 * c);
+            if (enc(&maps.m[c], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, addr, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return false;
+        }
     }
-    static bool attr = false;
-    if (!attr) {
-        if (cudaFuncSetAttribute(k_conv3d_fwd_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, kHSmem) != cudaSuccess)
+    auto kern = tma ? k_conv3d_fwd_halo<true> : k_conv3d_fwd_halo<false>;
+    static bool attr[2] = {false, false};
+    if (!attr[tma]) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kHSmem) != cudaSuccess)
             return false;
-        attr = true;
+        attr[tma] = true;
     }
     const int64_t n_tiles = (int64_t)xa.d * xa.h * ((xa.w + kTcM - 1) / kTcM);
     const unsigned grid = (unsigned)std::min<int64_t>(n_tiles, num_sms());
-    k_conv3d_fwd_halo<<<grid, 128, kHSmem, s>>>(maps, xa, cin, w, bias, relu, y, ya, yf);
+    kern<<<grid, 256, kHSmem, s>>>(maps, x, xa, cin, w, bias, relu, y, ya, yf);
     return true;
 }
 
@@ -1196,8 +1216,8 @@ int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *
         dim3 grid((unsigned)((nvox + 63) / 64), (unsigned)(cout / 64), (unsigned)xa.n);
         k_conv3d_fwd<64, 64><<<grid, 128, 0, s>>>(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf);
         g_conv_path = 0;
-    } else if (g_conv_tc >= 2 && launch_halo(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf, s)) {
-        g_conv_path = 3;  // batch-1 wide layers: tcgen05 on TMA-loaded halo tiles
+    } else if (g_conv_tc >= 2 && launch_halo(xp, xa, cin, wp, bias, cout, relu, yp, ya, yf, g_conv_tc == 3, s)) {
+        g_conv_path = g_conv_tc == 3 ? 3 : 5;  // batch-1 wide layers: tcgen05 on halo tiles
     } else if (ctas(128, 32) >= fill) {
         dim3 grid((unsigned)((nvox + 127) / 128), (unsigned)((cout + 31) / 32), (unsigned)xa.n);
         if (g_conv_tc && cout % 32 == 0 && ya.cstride % 8 == 0 && ya.coff % 8 == 0 && (uintptr_t)y % 16 == 0 &&
@@ -1217,7 +1237,7 @@ int srf_conv3d_fwd(const void *x, const int32_t xs[6], int32_t cin, const void *
 }
 
 int srf_set_conv_tc(int32_t mode) {
-    if (mode < 0 || mode > 2) return fail(SRF_EINVAL, "conv mode must be 0, 1 or 2");
+    if (mode < 0 || mode > 3) return fail(SRF_EINVAL, "conv mode must be 0, 1, 2 or 3");
     g_conv_tc = mode;
     return ok();
 }

@@ -92,9 +92,10 @@ def test_conv_forward_tile_shapes(cuda_lib, cnn):
 def test_conv_forward_tcgen05_tile(cuda_lib, cnn):
     """The tcgen05 kernels (accumulator in tensor memory) against the oracle and against the
     mma.sync kernels (mode 0): the 128-voxel x 32-channel K-step kernel (path 2, mode 1) and, for
-    batch-1 layers with W >= 96 and Cout = 32, the TMA halo-tile kernel (path 3, mode 2: one W-row
-    tile of 128 voxels plus a partial one, a single partial tile at W = 100); input and output
-    channel slices of wider buffers; a batch-2 layer keeps the split-K kernel (path 4)."""
+    batch-1 layers with W >= 96 and Cout = 32, the halo-tile kernel with cp.async halos (path 5,
+    mode 2) and with TMA halos (path 3, mode 3): one W-row tile of 128 voxels plus a partial one,
+    a single partial tile at W = 100; input and output channel slices of wider buffers; a batch-2
+    layer keeps the split-K kernel (path 4)."""
     from srf_gb300._lib import call, i32, ptr, stream_ptr
     from srf_gb300.surrogate import act
     rng = np.random.default_rng(9)
@@ -104,33 +105,35 @@ def test_conv_forward_tcgen05_tile(cuda_lib, cnn):
              ((1, 25, 40, 41), 32, 96, 0, 32, 2), ((1, 6, 5, 160), 32, 32, 0, 0, 3),
              ((1, 4, 3, 130), 96, 32, 16, 32, 3), ((1, 3, 4, 100), 16, 32, 0, 0, 3),
              ((2, 3, 4, 100), 16, 32, 0, 0, 4))
-    # mode 1 (the default) takes the K-step tcgen05 kernel, mode 2 also the halo kernel
+    # mode 1 (the default) takes the K-step tcgen05 kernel, modes 2 and 3 also the halo kernels
     try:
         for shape, cin, cout, xoff, yoff, path in cases:
             xbuf = _bf(rng.standard_normal(shape + (cin + xoff,))).to(dev)
             wt = _bf(rng.standard_normal((cout, 27, cin)) * 0.1).to(dev)
             bias = torch.as_tensor(rng.standard_normal(cout).astype(np.float32)).to(dev)
-            outs = []
-            for tc in (0, 2 if path == 3 else 1):
+            ref = cnn.conv3d(_np(xbuf)[..., xoff:], _np(wt), bias.cpu().numpy(), relu=True)
+            modes = {0: None, 1: path} if path != 3 else {0: None, 2: 5, 3: 3}
+            f0 = None
+            for tc, want in modes.items():
                 call("srf_set_conv_tc", i32(tc))
                 y = torch.zeros(shape + (cout + yoff,), dtype=torch.bfloat16, device=dev)
                 yf = torch.zeros(shape + (cout + yoff,), dtype=torch.float32, device=dev)
                 call("srf_conv3d_fwd", ptr(xbuf), act(xbuf, xoff), i32(cin), ptr(wt), ptr(bias), i32(cout),
                      i32(1), ptr(y), act(y, yoff), ptr(yf), s)
-                outs.append((y, yf))
-            used = ctypes.c_int32(-1)
-            call("srf_conv_last_path", ctypes.byref(used))
-            assert used.value == path, (shape, cin, cout, used.value)
-            status = ctypes.c_int32(0)
-            call("srf_conv_tc_status", ctypes.byref(status))
-            assert status.value == 0
-            ref = cnn.conv3d(_np(xbuf)[..., xoff:], _np(wt), bias.cpu().numpy(), relu=True)
-            (y0, f0), (y1, f1) = outs
-            got = f1.cpu().numpy()[..., yoff:]
-            assert rel_l2(got, ref) <= 1e-5, (shape, cin, cout)
-            assert rel_l2(f1.cpu().numpy()[..., yoff:], f0.cpu().numpy()[..., yoff:]) <= 1e-5  # FP32 sums in another order
-            assert rel_l2(_np(y1)[..., yoff:], ref) <= 4e-3
-            assert np.all(_np(y1)[..., :yoff] == 0)
+                got = yf.cpu().numpy()[..., yoff:]
+                if want is None:  # mma.sync
+                    f0 = got
+                    continue
+                used = ctypes.c_int32(-1)
+                call("srf_conv_last_path", ctypes.byref(used))
+                assert used.value == want, (shape, cin, cout, tc, used.value)
+                status = ctypes.c_int32(0)
+                call("srf_conv_tc_status", ctypes.byref(status))
+                assert status.value == 0
+                assert rel_l2(got, ref) <= 1e-5, (shape, cin, cout, tc)
+                assert rel_l2(got, f0) <= 1e-5  # FP32 sums in another order
+                assert rel_l2(_np(y)[..., yoff:], ref) <= 4e-3
+                assert np.all(_np(y)[..., :yoff] == 0)
     finally:
         call("srf_set_conv_tc", i32(1))
 
