@@ -119,14 +119,15 @@ class StudyBatch:
     def iteration_concurrent(self, n_streams: int = 8) -> None:
         """One iteration as independent per-study chains (each study's subset and update kernels
         in order) spread over ``n_streams`` streams forked from the current one and joined at the
-        end: the studies' kernels run side by side, each at the single-study kernel's efficiency,
-        and small studies fill the GPU together instead of one at a time."""
+        end (largest studies first, balanced by event count): the studies' kernels run side by
+        side, each at the single-study kernel's efficiency, and small studies fill the GPU together
+        instead of one at a time."""
         main = torch.cuda.current_stream(self.device)
         streams = self._streams(n_streams)
         for st_ in streams:
             st_.wait_stream(main)
-        for j, st in enumerate(self.studies):
-            with torch.cuda.stream(streams[j % len(streams)]):
+        for j, st in self._assignment(len(streams)):
+            with torch.cuda.stream(streams[j]):
                 per = st.lors.shape[0] // self.n_sub
                 for k in range(self.n_sub):
                     if per:
@@ -136,6 +137,18 @@ class StudyBatch:
                     st.state.update(st.emap, guard_zero=True)
         for st_ in streams:
             main.wait_stream(st_)
+
+    def _assignment(self, n: int):
+        """(stream, study) pairs: studies by event count, largest first, each onto the stream with
+        the fewest events so far (longest-processing-time-first), so that the chains end together
+        instead of one stream carrying several large studies."""
+        load = [0] * n
+        out = []
+        for st in sorted(self.studies, key=lambda s_: -int(s_.lors.shape[0])):
+            j = min(range(n), key=lambda i: load[i])
+            load[j] += int(st.lors.shape[0])
+            out.append((j, st))
+        return out
 
     def _streams(self, n: int) -> List[torch.cuda.Stream]:
         have = getattr(self, "_pool", [])
