@@ -237,7 +237,8 @@ def _half_cells(geo: CoarseGeometry):
         const = torch.stack([xm, ym, torch.cos(2 * th), torch.sin(2 * th), torch.cos(4 * th),
                              torch.sin(4 * th), pc], -1)
         pr = geo.pairs_dev.index_select(0, idx).long()
-        geo._half = (idx, L, const, pr[:, 0].contiguous(), pr[:, 1].contiguous())
+        len2 = ((L[:, 3] - L[:, 0]) ** 2 + (L[:, 4] - L[:, 1]) ** 2 + (L[:, 5] - L[:, 2]) ** 2)
+        geo._half = (idx, L, const, pr[:, 0].contiguous(), pr[:, 1].contiguous(), len2)
     return geo._half
 
 
@@ -255,12 +256,14 @@ def network_input(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor)
     rotation-equivariant in the views; the LOR's midpoint (x, y) / 300 mm, the 2nd and 4th
     harmonics of its direction and the plane coordinate locate each cell absolutely. Targets and
     predictions are in units of the emission scale, so the network is scale-free."""
-    idx, L, const, ca, cb = _half_cells(geo)
+    idx, L, const, ca, cb, len2 = _half_cells(geo)
     ic = geo.ic
-    p = kernels.project(L, kernels.xfast(emission), ic.center, ic.size)
-    len2 = ((L[:, 3] - L[:, 0]) ** 2 + (L[:, 4] - L[:, 1]) ** 2 + (L[:, 5] - L[:, 2]) ** 2)
+    # bin LORs cross at most ~90 slabs of the 64 x 64 x 32 grid: 8 lanes per LOR
+    # (measured 0.23 -> 0.18 ms for this function in the prediction graph)
+    with _lib.tuning(8, 4):
+        p = kernels.project(L, kernels.xfast(emission), ic.center, ic.size)
+        a = kernels.attenuation(L, kernels.xfast(mu), ic.center, ic.size)
     e = p * len2
-    a = kernels.attenuation(L, kernels.xfast(mu), ic.center, ic.size)
     scale = e.mean().clamp_min(1e-30)
     en = e / scale
     ea = en * a
