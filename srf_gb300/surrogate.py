@@ -530,10 +530,35 @@ def build_dataset(geo, seeds, log=None):
     return X, T, scales
 
 
+def corrected_targets(net: UNet3D, X: torch.Tensor, T0: torch.Tensor, batch: int = 4) -> torch.Tensor:
+    """Targets for training towards the spot-corrected estimate: per sample T0 / c, where
+    c = B beta is the smooth factor of the spot-check correction basis B (normalised to mean 1
+    over the bins, floored at 0.2) that maps the network's current prediction closest to T0 by
+    least squares over the real bins. The network then spends its capacity on what the
+    correction cannot supply."""
+    from .scatter_sinogram import PLANES, RADIAL, VIEWS, crop_sino, pad_sino
+    B = correction_basis(X.device).double()
+    out = torch.empty_like(T0)
+    n = X.shape[0]
+    for j in range(0, n, batch):
+        k = min(batch, n - j)
+        p = crop_sino(net.forward(X[j:j + k].contiguous())).double()
+        t = crop_sino(T0[j:j + k]).double()
+        A = torch.einsum("kb,sb,lb->skl", B, p * p, B)
+        r = torch.einsum("kb,sb->sk", B, p * t)
+        beta = torch.linalg.solve(A + 1e-12 * torch.eye(B.shape[0], dtype=A.dtype, device=A.device), r)
+        c = beta @ B
+        c = (c / c.mean(dim=1, keepdim=True)).clamp_min(0.2)
+        out[j:j + k] = pad_sino((t / c).reshape(k, PLANES - 1, RADIAL, VIEWS).float())
+    return out
+
+
 def train(net: UNet3D, X: torch.Tensor, T: torch.Tensor, mask: torch.Tensor, epochs: int,
-          batch: int = 4, lr: float = 2e-3, seed: int = 0, log=None, every=None) -> List[float]:
+          batch: int = 4, lr: float = 2e-3, seed: int = 0, log=None, every=None,
+          retarget=None) -> List[float]:
     """Adam on the masked relative squared error, cosine-decayed learning rate; ``every(epoch)``
-    runs after each epoch (monitoring)."""
+    runs after each epoch (monitoring); ``retarget(epoch)`` may return new targets for the
+    following epochs."""
     n = X.shape[0]
     g = torch.Generator().manual_seed(seed)
     inv_den = 1.0 / (T * T * mask).sum(dim=(1, 2, 3)).clamp_min(1e-30)
@@ -559,7 +584,24 @@ def train(net: UNet3D, X: torch.Tensor, T: torch.Tensor, mask: torch.Tensor, epo
             log(f"epoch {ep + 1}/{epochs} loss(first batch) {hist[-1]:.5f}")
         if every:
             every(ep + 1)
+        if retarget is not None and ep + 1 < epochs:
+            nt = retarget(ep + 1)
+            if nt is not None:
+                T = nt
+                inv_den = 1.0 / (T * T * mask).sum(dim=(1, 2, 3)).clamp_min(1e-30)
     return hist
+
+
+def evaluate_corrected(sur: "ScatterSurrogate", seeds) -> List[float]:
+    """Full-resolution relative L2 of the spot-corrected estimate against the full SSS."""
+    from .scatter_sinogram import random_phantom, sss_sinogram
+    errs = []
+    for sd in seeds:
+        em, mu = random_phantom(int(sd), device=sur.geo.device)
+        ref = sss_sinogram(sur.geo, em, mu)
+        p, _ = sur.estimate(em, mu, fallback=False)
+        errs.append(float((torch.linalg.vector_norm(p - ref) / torch.linalg.vector_norm(ref)).item()))
+    return errs
 
 
 def evaluate(sur: "ScatterSurrogate", seeds) -> List[float]:
@@ -628,6 +670,9 @@ def main(argv=None) -> None:
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--channels", default="32,64,96")
+    ap.add_argument("--corrected", type=int, default=0,
+                    help="after this many epochs, train towards the spot-corrected estimate "
+                         "(targets refreshed every 5 epochs); 0: plain targets")
     ap.add_argument("--calibrate", default=None, help="write the guard calibration to this file")
     ap.add_argument("--studies", type=int, default=40, help="calibration phantoms")
     a = ap.parse_args(argv)
@@ -657,16 +702,29 @@ def main(argv=None) -> None:
     def every(ep):
         if ep % 5 == 0 or ep == a.epochs:
             e = evaluate(sur, mon)
-            log(f"epoch {ep}: held-out rel L2 mean {sum(e) / len(e):.4f} max {max(e):.4f}")
+            c = evaluate_corrected(sur, mon)
+            log(f"epoch {ep}: held-out rel L2 mean {sum(e) / len(e):.4f} max {max(e):.4f}; "
+                f"corrected mean {sum(c) / len(c):.4f} max {max(c):.4f}")
+
+    T0 = T
+
+    def retarget(ep):
+        if a.corrected and ep >= a.corrected and (ep - a.corrected) % 5 == 0:
+            log(f"epoch {ep}: targets towards the corrected estimate")
+            return corrected_targets(net, X, T0, a.batch)
+        return None
 
     t0 = time.time()
-    hist = train(net, X, T, mask, a.epochs, a.batch, a.lr, log=log, every=every)
+    hist = train(net, X, T, mask, a.epochs, a.batch, a.lr, log=log, every=every, retarget=retarget)
     torch.cuda.synchronize()
     t_train = time.time() - t0
-    del X, T
+    del X, T, T0
     errs = evaluate(sur, range(1_000_000, 1_000_000 + a.held_out))
+    cerrs = evaluate_corrected(sur, range(1_000_000, 1_000_000 + min(a.held_out, 100)))
     meta = {"target_scale": k, "train_studies": a.train, "epochs": a.epochs, "train_s": t_train,
-            "held_out_mean_rel_l2": sum(errs) / len(errs), "held_out_max_rel_l2": max(errs)}
+            "corrected_from_epoch": a.corrected,
+            "held_out_mean_rel_l2": sum(errs) / len(errs), "held_out_max_rel_l2": max(errs),
+            "held_out_corrected_mean_rel_l2": sum(cerrs) / len(cerrs)}
     save_weights(net, a.out, meta)
     print(json.dumps({**meta, "loss_history": hist}))
 

@@ -214,3 +214,32 @@ def test_surrogate_guard_threshold_rule():
     assert guard_threshold(recs, 0.01, 1.0) == 0.12       # all within 1 %: the largest seen
     assert guard_threshold([(0.02, 0.02)], 0.01, 0.75) == 0.0
     assert guard_threshold([], 0.01, 0.75) == 0.0
+
+
+def test_surrogate_corrected_targets_remove_a_smooth_factor():
+    """corrected_targets: when the prediction is the target divided by a smooth factor of the
+    correction basis, the new target is the prediction itself (scaled so that the factor has
+    mean 1 over the bins), i.e. the factor the spot-check correction supplies is taken out."""
+    import torch
+    from srf_gb300.scatter_sinogram import PAD_GRID, crop_sino, pad_sino, PLANES, RADIAL, VIEWS
+    from srf_gb300.surrogate import correction_basis, corrected_targets
+    g = torch.Generator().manual_seed(3)
+    B = correction_basis("cpu").double()
+    nb = B.shape[1]
+    t_flat = 0.5 + torch.rand((2, nb), generator=g, dtype=torch.float64)
+    beta = torch.tensor([[1.0, 0.2, -0.1, 0.05, 0.1, 0.1, -0.05, 0.02, 0.03],
+                         [2.0, -0.3, 0.2, 0.1, -0.2, 0.0, 0.1, -0.1, 0.05]], dtype=torch.float64)
+    c = beta @ B
+    pred_flat = t_flat / c
+    T0 = pad_sino(t_flat.reshape(2, PLANES - 1, RADIAL, VIEWS).float())
+    pred = pad_sino(pred_flat.reshape(2, PLANES - 1, RADIAL, VIEWS).float())
+
+    class Fixed:
+        def forward(self, x):
+            return pred[int(x[0, 0]): int(x[0, 0]) + x.shape[0]]
+
+    X = torch.arange(2, dtype=torch.float32).reshape(2, 1)
+    got = crop_sino(corrected_targets(Fixed(), X, T0, batch=1)).double()
+    want = pred_flat * c.mean(dim=1, keepdim=True)
+    assert got.shape == (2, nb) and PAD_GRID[0] >= PLANES
+    assert float(((got - want).norm() / want.norm())) < 1e-5
