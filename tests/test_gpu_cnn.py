@@ -94,8 +94,9 @@ def test_conv_forward_tcgen05_tile(cuda_lib, cnn):
     mma.sync kernels (mode 0): the 128-voxel x 32-channel K-step kernel (path 2, mode 1) and, for
     batch-1 layers with W >= 96 and Cout = 32, the halo-tile kernel with cp.async halos (path 5,
     mode 2) and with TMA halos (path 3, mode 3): one W-row tile of 128 voxels plus a partial one,
-    a single partial tile at W = 100; input and output channel slices of wider buffers; a batch-2
-    layer keeps the split-K kernel (path 4)."""
+    a single partial tile at W = 100; input and output channel slices of wider buffers; a small
+    batch-2 layer keeps the split-K kernel (path 4), a larger one takes the K-step kernel with
+    the batch index in the grid (as in training)."""
     from srf_gb300._lib import call, i32, ptr, stream_ptr
     from srf_gb300.surrogate import act
     rng = np.random.default_rng(9)
@@ -104,7 +105,7 @@ def test_conv_forward_tcgen05_tile(cuda_lib, cnn):
     cases = (((1, 25, 40, 40), 16, 32, 0, 0, 2), ((1, 25, 40, 40), 96, 32, 16, 32, 2),
              ((1, 25, 40, 41), 32, 96, 0, 32, 2), ((1, 6, 5, 160), 32, 32, 0, 0, 3),
              ((1, 4, 3, 130), 96, 32, 16, 32, 3), ((1, 3, 4, 100), 16, 32, 0, 0, 3),
-             ((2, 3, 4, 100), 16, 32, 0, 0, 4))
+             ((2, 3, 4, 100), 16, 32, 0, 0, 4), ((2, 13, 40, 40), 32, 32, 16, 32, 2))
     # mode 1 (the default) takes the K-step tcgen05 kernel, modes 2 and 3 also the halo kernels
     try:
         for shape, cin, cout, xoff, yoff, path in cases:
