@@ -867,7 +867,28 @@ def run_surrogate(a, ws, rank, local):
         fb5 += int(info["spot_rel_l2"] > 0.05)
     img_sss = study.reconstruct(study.sss)
     img_sur = study.reconstruct(sur.estimate(study.emission, study.mu, fallback=False)[0])
+    # the reference's SSS core runs on the CPU (numba); its C restatement (the oracle) on one host
+    # core over a 2,000-bin sample of the first held-out phantom, extrapolated to every bin
+    cpu_sss = None
+    if rank == 0 and not a.no_cpu:
+        import numpy as np
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        from srf_gb300.scatter_sinogram import sss_args, sss_tables
+        O.build()
+        em0, mu0 = random_phantom(seeds[0], device=dev)
+        sumup, atten = sss_tables(geo, em0, mu0, geo.vpos_dev)
+        sample = np.ascontiguousarray(geo.pairs[np.random.default_rng(a.seed).choice(geo.n_bins(), 2000, replace=False)])
+        t0 = time.perf_counter()
+        O.sss(sample, geo.vpos, geo.scatter_points.astype(np.float32), sumup.cpu().numpy(), atten.cpu().numpy(),
+              mu0.cpu().numpy(), list(geo.ic.size), *sss_args(geo))
+        t_cpu = (time.perf_counter() - t0) * geo.n_bins() / len(sample)
+        cpu_sss = {"core_s_estimate": t_cpu, "cores": 1, "kind": "port",
+                   "sample": "2000 of 827,424 bins, SSS core only (preprocessing excluded)",
+                   "network_path_speedup": None}
     med_sss, med_sur, med_net = statistics.median(t_sss), statistics.median(t_sur), statistics.median(t_net)
+    if cpu_sss is not None:
+        cpu_sss["network_path_speedup"] = cpu_sss["core_s_estimate"] / med_net
     mean_sss, mean_sur = sum(t_sss) / len(t_sss), sum(t_sur) / len(t_sur)
     if rank == 0:
         print(json.dumps({
@@ -892,6 +913,7 @@ def run_surrogate(a, ws, rank, local):
             "spot_rel_l2_mean": sum(spot) / len(spot),
             "spot_rel_l2_uncorrected_mean": sum(spot_raw) / len(spot_raw), "fallbacks": fallbacks,
             "fallbacks_at_5pct_spot": fb5,
+            "sss_cpu_reference_port": cpu_sss,
             "osem": {"events": int(study.events.shape[0]), "scatter_fraction": study.sf,
                      "iterations": study.n_iter, "subsets": study.n_sub,
                      "image_rel_l2_surrogate_vs_sss": rel(img_sur, img_sss),

@@ -164,10 +164,10 @@ def sss_sinogram(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor,
                      inv.reshape(-1, 2).to(torch.int32), low, high, resolution)
 
 
-def sss_pairs(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor, cpos: torch.Tensor,
-              pairs: torch.Tensor, low: int = 350, high: int = 650, resolution: float = 0.15) -> torch.Tensor:
-    """SSS of crystal pairs given as int32 indices into the crystal positions ``cpos`` (m, 3):
-    preprocessing of those m crystals, then srf_sss. No host synchronisation."""
+def sss_tables(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor, cpos: torch.Tensor):
+    """The SSS preprocessing (preprocess.py:21-43) of crystals ``cpos`` (m, 3): per crystal and
+    scatter point the emission line integral x |LOR|^2 and the attenuation factor, (m, n_points)
+    each, on the GPU projector."""
     sp = geo.scatter_points_dev
     ic = geo.ic
     m, k = cpos.shape[0], sp.shape[0]
@@ -180,10 +180,23 @@ def sss_pairs(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor, cpo
         atten = kernels.attenuation(Ld, kernels.xfast(mu), ic.center, ic.size).reshape(m, k)
     len2 = ((Ld[:, 3] - Ld[:, 0]) ** 2 + (Ld[:, 4] - Ld[:, 1]) ** 2 + (Ld[:, 5] - Ld[:, 2]) ** 2)
     sumup = (p * len2).reshape(m, k)
+    return sumup.contiguous(), atten.contiguous()
+
+
+def sss_args(geo: CoarseGeometry, low: int = 350, high: int = 650, resolution: float = 0.15):
+    """The scanner and energy arguments of srf_sss for the coarse geometry (after umap, umap_size)."""
     s = geo.scanner
-    sc, _ = kernels.sss(pairs.contiguous(), cpos.contiguous(), sp, sumup.contiguous(), atten.contiguous(),
-                        mu.contiguous(), list(ic.size), s.nb_blocks_per_ring * s.blocks.shape[1],
-                        s.nb_blocks_per_ring, list(s.blocks.shape), low, high, resolution)
+    return (s.nb_blocks_per_ring * s.blocks.shape[1], s.nb_blocks_per_ring, list(s.blocks.shape), low, high,
+            resolution)
+
+
+def sss_pairs(geo: CoarseGeometry, emission: torch.Tensor, mu: torch.Tensor, cpos: torch.Tensor,
+              pairs: torch.Tensor, low: int = 350, high: int = 650, resolution: float = 0.15) -> torch.Tensor:
+    """SSS of crystal pairs given as int32 indices into the crystal positions ``cpos`` (m, 3):
+    preprocessing of those m crystals, then srf_sss. No host synchronisation."""
+    sumup, atten = sss_tables(geo, emission, mu, cpos)
+    sc, _ = kernels.sss(pairs.contiguous(), cpos.contiguous(), geo.scatter_points_dev, sumup, atten,
+                        mu.contiguous(), list(geo.ic.size), *sss_args(geo, low, high, resolution))
     return sc
 
 
