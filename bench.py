@@ -76,6 +76,7 @@ def workload_config(a):
         "workload": "tof_listmode_osem_clinical",
         "events": int(a.events), "image": [200, 200, 109], "voxel_mm": [2.04, 2.04, 2.03],
         "crystals": 32448, "subsets": a.subsets, "tof_fwhm_ps": 530.0, "tof_nsigma": a.nsigma,
+        "subset_order": "interleaved: event i in subset i mod subsets (OsemFullTof subsets='interleaved')",
         "step": "one full OSEM iteration (all subsets)",
         "l2": "inputs larger than L2 (LOR stream 560 MB per iteration)",
         "lanes_per_lor": a.lanes,
@@ -969,7 +970,7 @@ def run_clinical(a, ws, rank, local):
     from srf_gb300 import _lib, kernels
     from srf_gb300._lib import SRF_RATIO_DIV_NO_NAN
     from srf_gb300.data import Emap, Listmode, Lors
-    from srf_gb300.distributed import ShardedOsem, subset_shards
+    from srf_gb300.distributed import ShardedOsem, shard_range
     from srf_gb300.geometry import block_full_crystal_table
     from srf_gb300.recon import OsemFullTof
 
@@ -1023,19 +1024,18 @@ def run_clinical(a, ws, rank, local):
         h2d_gbps = host_lors.numel() * 4 / (h0.elapsed_time(h1) / 1000.0) / 1e9
         del scratch
 
-    # subset order: a seeded permutation, each subset contiguous; this rank keeps its shards
-    perm = torch.as_tensor(np.random.default_rng(a.seed).permutation(n), device=dev)
-    lors = lors.index_select(0, perm)
-    del perm
-    ranges = subset_shards(n, n_sub, rank, ws)
+    # interleaved subsets: subset k is events k, k + n_sub, ... of the list in event order (a
+    # strided view, no reordering); this rank keeps its contiguous share of each subset
+    n_per = n // n_sub
+    n_used = n_per * n_sub
+    lo, hi = shard_range(n_per, rank, ws)
+    shard_lors = [lors[k:n_used:n_sub][lo:hi] for k in range(n_sub)]
+    mine = n_sub * (hi - lo)
 
     # exact LOR-voxel visits of one iteration (all ranks' events)
-    n_used = (n // n_sub) * n_sub
     p_fwd = kernels.count_pairs(lors[:n_used], ic.shape, ic.center, ic.size, rules=0, tof=tof, tof_nsigma=a.nsigma)
     p_bwd = kernels.count_pairs(lors[:n_used], ic.shape, ic.center, ic.size, rules=1, tof=tof, tof_nsigma=a.nsigma)
     updates_per_iter = p_fwd + p_bwd
-    shard_lors = [lors[lo:hi] for lo, hi in ranges]
-    mine = sum(hi - lo for lo, hi in ranges)
 
     st = kernels.SubsetState(ic.shape, ic.center, ic.size, dev)
     drv = ShardedOsem(st)
@@ -1113,15 +1113,15 @@ def run_clinical(a, ws, rank, local):
     sens_term = float((emap.double() * st.x.double()).sum().item())
     del llst
 
-    # end to end through the drop-in: OsemFullTof(1 iteration) on pinned host LORs and values --
-    # host-to-device copies, the device permutation, every subset step (with N ranks: this
-    # rank's shards and the per-subset all-reduce) -- and the image read back into pinned host
-    # memory, every step
+    # end to end through the drop-in: OsemFullTof(1 iteration, interleaved subsets) on pinned host
+    # LORs and values -- host-to-device copies, the values regrouped by subset, every subset step
+    # (with N ranks: this rank's shards and the per-subset all-reduce) -- and the image read back
+    # into pinned host memory, every step
     e2e = None
     if host_lors is not None:
         emap_img = Emap(emap, list(ic.center), list(ic.size))
         rec = OsemFullTof(1, n_sub, ic, sc, Listmode(host_y, Lors(host_lors)), emap_img,
-                          tof_nsigma=a.nsigma, seed=a.seed, sharded=ws > 1)
+                          tof_nsigma=a.nsigma, seed=a.seed, sharded=ws > 1, subsets="interleaved")
         out_host = torch.empty(ic.shape, dtype=torch.float32, pin_memory=True)
 
         def e2e_step():

@@ -7,7 +7,9 @@
 * ``OsemFull(n_iter, n_sub, image_config, scanner, listmode, atten_corr, scatter_corr, norm_corr,
   psf_corr, emap, image)()``                                 srfnef/functions/osem_full.py:30-87
 * ``OsemFullTof`` -- not in the reference (it has no TOF OSEM): OsemFull's subset loop with
-  MlemFullTof's update rule, cyclic subsets of a seeded permutation and an emap scaled per subset.
+  MlemFullTof's update rule and an emap scaled per subset; cyclic subsets of a seeded
+  permutation (``subsets='random'``), or interleaved subsets (``subsets='interleaved'``: event i
+  in subset i mod n_sub), which need no reordering of the list-mode data on the device.
 
 Update rules, as the reference (float32 throughout):
   Mlem        r = y / (p + mean(y)*1e-8)       emap zeros -> 1e8
@@ -52,6 +54,13 @@ def _device_permutation(seed: int, n: int, dev) -> torch.Tensor:
         perm = torch.as_tensor(np.random.default_rng(seed).permutation(n), device=dev)
         _PERMS[key] = perm
     return perm
+
+
+def _by_subset(v: torch.Tensor, n_sub: int) -> torch.Tensor:
+    """(n_sub, n // n_sub): row k holds events k, k + n_sub, ... of a per-event vector (the
+    remainder events are left out, as the subset loop does)."""
+    n_per = v.shape[0] // n_sub
+    return v[:n_per * n_sub].reshape(n_per, n_sub).t().contiguous()
 
 
 def _emap_dev(emap) -> torch.Tensor:
@@ -214,23 +223,33 @@ class OsemFullTof(_NefLike):
     add: Any = None                      # per-event additive expected counts (e.g. scatter)
     sharded: bool = False                # split each subset's events over the process group's ranks
     group: Any = None                    # torch.distributed group (None: the default group)
+    subsets: str = "random"              # 'random' (seeded permutation) or 'interleaved'
 
     def prepare(self):
-        """Device-resident inputs: LORs and values permuted into subset order once. Host tensors
-        in pinned memory are copied on a side stream, overlapping the device work already queued
-        (with repeated calls, the previous reconstruction); the caller keeps them unchanged until
-        the call's result is read. The permutation is applied on the device."""
+        """Device-resident inputs in subset order. Host tensors in pinned memory are copied on a
+        side stream, overlapping the device work already queued (with repeated calls, the previous
+        reconstruction); the caller keeps them unchanged until the call's result is read.
+        'random': LORs and values permuted on the device. 'interleaved': the LORs stay in event
+        order (subset k is the strided view of events k, k + n_sub, ...) and only the values and
+        the additive term, one float per event, are regrouped by subset."""
+        if self.subsets not in ("random", "interleaved"):
+            raise ValueError(f"subsets must be 'random' or 'interleaved', got {self.subsets!r}")
         lm = PetEcatListmodeTrans(self.scanner)(self.listmode) if self.snap else self.listmode
         dev = device()
         n = len(lm)
         lors = to_dev_overlapped(lm.lors.data)
         y = to_dev_overlapped(lm.data)
-        perm = _device_permutation(self.seed, n, dev)
-        lors = lors.index_select(0, perm)
-        y = y.index_select(0, perm)
-        # a frozen record: the permuted additive term is cached beside the fields
-        object.__setattr__(self, "_add", None if self.add is None
-                           else to_dev(self.add).index_select(0, perm).contiguous())
+        add = None if self.add is None else to_dev(self.add)
+        if self.subsets == "random":
+            perm = _device_permutation(self.seed, n, dev)
+            lors = lors.index_select(0, perm)
+            y = y.index_select(0, perm)
+            add = None if add is None else add.index_select(0, perm).contiguous()
+        else:
+            y = _by_subset(y, self.n_sub)
+            add = None if add is None else _by_subset(add, self.n_sub)
+        # a frozen record: the reordered additive term is cached beside the fields
+        object.__setattr__(self, "_add", add)
         scale = (1.0 / self.n_sub) if self.emap_scale is None else self.emap_scale
         em = (_emap_dev(self.emap) * scale)
         return lors, y, em
@@ -238,23 +257,32 @@ class OsemFullTof(_NefLike):
     def run(self, lors: torch.Tensor, y: Optional[torch.Tensor], em: torch.Tensor,
             state: Optional[kernels.SubsetState] = None, n_iter: Optional[int] = None,
             track_loglik: bool = False) -> kernels.SubsetState:
-        """``n_iter`` passes over the subsets of the subset-ordered events. With ``sharded``, this
-        rank processes its contiguous share of every subset and the ranks' backprojections are
-        summed before each update (every rank ends with the same image)."""
+        """``n_iter`` passes over the subsets of the events as ``prepare`` returns them. With
+        ``sharded``, this rank processes its contiguous share of every subset and the ranks'
+        backprojections are summed before each update (every rank ends with the same image)."""
         ic = self.image_config
         st = state or kernels.SubsetState(ic.shape, ic.center, ic.size, lors.device)
         n = lors.shape[0]
         rank, world = distributed.world_of(self.group) if self.sharded else (0, 1)
-        ranges = distributed.subset_shards(n, self.n_sub, rank, world)
         driver = distributed.ShardedOsem(st, self.group) if self.sharded else None
         tof = (self.scanner.tof.tof_bin, self.scanner.tof.tof_sigma2)
         add = getattr(self, "_add", None)
+        steps = []  # (LORs, values, additive term) of this rank's shard of each subset
+        if self.subsets == "interleaved":
+            n_per = n // self.n_sub
+            lo, hi = distributed.shard_range(n_per, rank, world)
+            for k in range(self.n_sub):
+                view = lors[k:n_per * self.n_sub:self.n_sub]  # events k, k + n_sub, ...
+                steps.append((view[lo:hi], None if y is None else y[k, lo:hi],
+                              None if add is None else add[k, lo:hi]))
+        else:
+            for lo, hi in distributed.subset_shards(n, self.n_sub, rank, world):
+                steps.append((lors[lo:hi], None if y is None else y[lo:hi],
+                              None if add is None else add[lo:hi]))
         for _ in range(self.n_iter if n_iter is None else n_iter):
-            for lo, hi in ranges:
-                sl = slice(lo, hi)
-                st.subset(lors[sl], None if y is None else y[sl], rule=SRF_RATIO_DIV_NO_NAN,
-                          eps=1e-5, tof=tof, tof_nsigma=self.tof_nsigma, track_loglik=track_loglik,
-                          add=None if add is None else add[sl])
+            for l_k, y_k, a_k in steps:
+                st.subset(l_k, y_k, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5, tof=tof,
+                          tof_nsigma=self.tof_nsigma, track_loglik=track_loglik, add=a_k)
                 if driver is not None:
                     driver.reduce()
                 st.update(em, guard_zero=True)

@@ -161,3 +161,29 @@ def test_osem_update_paths_bit_exact(cuda_lib, shape, offset):
     got_t = dxt.cpu().numpy().reshape(nz, nx, ny)
     assert np.array_equal(got_t.view(np.int32), np.ascontiguousarray(want.transpose(0, 2, 1)).view(np.int32))
     assert not dbp.any().item() and not dbpt.any().item()
+
+
+def test_osem_tof_interleaved_subsets_match_oracle(cuda_lib, oracle, small_case, emap_small):
+    """subsets='interleaved': subset k holds events k, k + n_sub, ... (no reordering of the LORs;
+    the values and the additive term are regrouped by subset); uneven n (the remainder is left
+    out), per-event values and an additive term."""
+    import srf_gb300 as nef
+    sc, ic, lors = small_case["scanner"], small_case["ic"], small_case["lors"]
+    n_sub = 4
+    lors = np.ascontiguousarray(lors[: (len(lors) // n_sub) * n_sub - 3])  # 3 events past the last full row
+    rng = np.random.default_rng(12)
+    y = (0.5 + rng.random(len(lors))).astype(np.float32)
+    add = (rng.random(len(lors)) * 1e-3).astype(np.float32)
+    lm = nef.Listmode(y, nef.Lors(lors))
+    em = nef.Emap(emap_small, ic.center, ic.size)
+    out = nef.OsemFullTof(2, n_sub, ic, sc, lm, em, tof_nsigma=3.0, add=add, subsets="interleaved")()
+    n_used = (len(lors) // n_sub) * n_sub
+    order = np.concatenate([np.arange(k, n_used, n_sub) for k in range(n_sub)] +
+                           [np.arange(n_used, len(lors))])
+    ref = oracle.osem(lors, y, emap_small, ic.shape, ic.center, ic.size, 2 * n_sub, n_sub, order,
+                      rule="full_tof", emap_scale=1.0 / n_sub, guard=True, subset_index="mod",
+                      tof=True, tof_bin=sc.tof.tof_bin, tof_sigma2=sc.tof.tof_sigma2,
+                      tof_nsigma=3.0, add=add)
+    assert rel_l2(out.data, ref) <= TOL
+    with pytest.raises(ValueError):
+        nef.OsemFullTof(1, n_sub, ic, sc, lm, em, subsets="blocks")()
