@@ -36,9 +36,9 @@ sys.path.insert(0, ROOT)
 METRIC = "TOF OSEM s/iter & LOR-voxel updates/s on 1 GB300 vs plain, rel L2 err ≤1e-5"
 UNIT = "LOR-voxel updates/s"
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes (read + write) of one k_osem_subset launch of this workload (2e6 TOF LORs, clinical
-# image), from ncu: profiles/k_osem_subset_tof_clinical_2M_lors.txt
-NCU_TRAFFIC_SUBSET = 124_260_096
+# DRAM bytes (read + write) of one k_osem_subset launch of this workload (2e6 TOF LORs of an
+# interleaved subset, clinical image), from ncu: profiles/k_osem_subset_tof_clinical_2M_lors.txt
+NCU_TRAFFIC_SUBSET = 187_251_712
 
 
 def parse():
@@ -694,7 +694,8 @@ def run_components(a, ws, rank, local):
 
 def run_profile(a, ws, rank, local):
     """Subset steps of the clinical workload without the sensitivity image and visit counts
-    (emap = 1): warmup + steps iterations of n_subsets (subset, update) launch pairs."""
+    (emap = 1): warmup + steps iterations of n_subsets (subset, update) launch pairs, on the
+    headline's interleaved subsets (strided views of the events)."""
     import torch
     from srf_gb300 import _lib, kernels
     from srf_gb300._lib import SRF_RATIO_DIV_NO_NAN
@@ -709,7 +710,7 @@ def run_profile(a, ws, rank, local):
     st = kernels.SubsetState(ic.shape, ic.center, ic.size, dev)
     for _ in range(a.warmup + a.steps):
         for k in range(a.subsets):
-            st.subset(lors[k * n_per:(k + 1) * n_per], None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5,
+            st.subset(lors[k:n_per * a.subsets:a.subsets], None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5,
                       tof=tof, tof_nsigma=a.nsigma)
             st.update(em, guard_zero=True)
     torch.cuda.synchronize()
