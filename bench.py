@@ -1146,8 +1146,8 @@ def run_clinical(a, ws, rank, local):
                "h2d_bytes_per_step": int(ws * (host_lors.numel() * 4 + host_y.numel() * 4)),
                "d2h_bytes_per_step": int(ws * out_host.numel() * 4), "ms_per_step": e_ms,
                "h2d_gbps_single_copy": h2d_gbps,
-               "path": "srf_gb300.OsemFullTof(1 iteration, %d subsets)() per step on pinned host "
-                       "LORs; image copied back" % n_sub}
+               "path": "srf_gb300.OsemFullTof(1 iteration, %d interleaved subsets)() per step on "
+                       "pinned host LORs; image copied back" % n_sub}
         del rec
     host_lors = host_y = None
 
