@@ -7,7 +7,9 @@ Scanner: 32,448 crystals (424/444 mm radii, 48 blocks of 13 x 13 crystals, 4 blo
 At this size an exact (untruncated) TOF LOR spans up to 200 slabs. The fused kernel's default
 variant (32 lanes x 4 slabs per chunk) therefore walks many LORs in several chunks and recomputes
 their candidates for the backprojection. At 3 sigma every LOR fits one chunk, so the
-backprojection reuses the projection's candidates. Both paths are compared here.
+backprojection reuses the projection's candidates. Both paths are compared here. At 4 sigma a
+LOR spans up to about 133 slabs, so LORs that fit one chunk and LORs that take two meet in the
+same batch of 32.
 
 Tolerance: 1e-5 relative L2 (FP32), as the small-scanner parity tests.
 """
@@ -113,7 +115,7 @@ def test_clinical_nontof_projection_and_backprojection(cuda_lib, oracle, clinica
     assert rel_l2(got_b, ref_b) <= TOL
 
 
-@pytest.mark.parametrize("nsigma", [0.0, 3.0])
+@pytest.mark.parametrize("nsigma", [0.0, 3.0, 4.0])
 def test_clinical_osem_subset_step(cuda_lib, oracle, clinical, nsigma):
     """One fused subset step (projection, MlemFullTof's ratio, backprojection) and the update,
     under the default tuning, with the FP64 log-likelihood sum y log(p + eps)."""
