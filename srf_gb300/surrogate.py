@@ -131,8 +131,13 @@ class UNet3D:
 
     def forward(self, inp: torch.Tensor) -> torch.Tensor:
         """inp: (N, D, H, W, 16) bfloat16 -> (N, 2D, 2H, 2W) float32."""
+        if inp.dim() != 5 or inp.shape[-1] != self.IN_CH or inp.dtype != BF16:
+            raise ValueError(f"expected (N, D, H, W, {self.IN_CH}) bfloat16, got {tuple(inp.shape)} {inp.dtype}")
+        dv = self.device
+        if inp.device.type != dv.type or (dv.index is not None and inp.device.index != dv.index) \
+                or not inp.is_contiguous():
+            raise ValueError(f"input must be a contiguous tensor on {self.device}")
         n, d, h, w, c = inp.shape
-        assert c == self.IN_CH and inp.dtype == BF16
         self._alloc(n, (d, h, w))
         self._inp = inp
         b, s = self.buf, stream_ptr(self.device)
