@@ -187,3 +187,36 @@ def test_osem_tof_interleaved_subsets_match_oracle(cuda_lib, oracle, small_case,
     assert rel_l2(out.data, ref) <= TOL
     with pytest.raises(ValueError):
         nef.OsemFullTof(1, n_sub, ic, sc, lm, em, subsets="blocks")()
+
+
+@pytest.mark.parametrize("tof, nsigma, n_ev", [(False, 0.0, 20000), (True, 0.0, 20000), (True, 3.0, 20000),
+                                                (True, 3.0, 33), (False, 0.0, 33)])
+def test_osem_subset_step_nonsquare_voxels(cuda_lib, oracle, small_case, tof, nsigma, n_ev):
+    """One fused subset step and the update on a grid with dy != dx (2.0 x 1.8 mm, off-centre): the
+    subset kernel's variant with the reference's in-plane division by dy for x-dominant LORs
+    (siddon.cu.cc:59-73), against the oracle's projection, MlemFullTof ratio and backprojection;
+    also with 33 events (a second warp batch holding one LOR). The bound is an image-level one: the
+    axial crossing fractions carry a few ulp of the linear z form, which a single LOR's image does
+    not average (one non-TOF LOR measured 1.4e-5)."""
+    import torch
+    from srf_gb300 import kernels
+    from srf_gb300._lib import SRF_RATIO_DIV_NO_NAN
+    sc, lors = small_case["scanner"], np.ascontiguousarray(small_case["lors"][:n_ev])
+    sh, c, s = [48, 40, 12], [1.5, -2.0, 0.5], [96.0, 72.0, 30.0]
+    rng = np.random.default_rng(31)
+    img = (0.2 + rng.random(sh)).astype(np.float32)
+    emap = (0.5 + rng.random(sh)).astype(np.float32)
+    emap[0, 0, :] = 0.0  # guarded voxels
+    t = (sc.tof.tof_bin, sc.tof.tof_sigma2) if tof else None
+    dev = torch.device("cuda", 0)
+    st = kernels.SubsetState(sh, c, s, dev, x0=torch.as_tensor(img, device=dev))
+    st.subset(torch.as_tensor(lors, device=dev), None, rule=SRF_RATIO_DIV_NO_NAN, eps=1e-5, tof=t,
+              tof_nsigma=nsigma)
+    st.update(kernels.xfast(torch.as_tensor(emap, device=dev)), guard_zero=True)
+    got = st.x.contiguous().cpu().numpy()
+    kw = dict(tof=True, tof_bin=t[0], tof_sigma2=t[1], tof_nsigma=nsigma) if tof else {}
+    p = oracle.projection(img, lors, sh, c, s, **kw)
+    r = oracle.ratio(np.ones(len(lors), np.float32), p, "full_tof")
+    bp = oracle.backprojection(r, lors, sh, c, s, **kw)
+    want = (img * bp / oracle.guard_emap(emap)).astype(np.float32)
+    assert rel_l2(got, want) <= TOL
