@@ -287,13 +287,43 @@ __device__ __forceinline__ void lean_slab(const LeanRec &E, const LeanAxes &ax, 
     w[0] = w0; w[1] = w1; w[2] = w2;
 }
 
+// The first N groups of a chunk, all inside [ilo, ihi], as straight-line code (no branch
+// between the groups, so their instruction streams interleave); groups N..U-1 are zero.
+template <bool TOF, int U, int G, bool QDIV, int N>
+__device__ __forceinline__ void lean_interior_groups(const LeanRec &E, const LeanAxes &ax, int c0, int whi,
+                                                     float ppmax, float pp0, int lane, int32_t (&o)[U][3],
+                                                     float (&w)[U][3]) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (u < N) {
+            const int ip = c0 + G * u + lane;
+            const bool act = ip <= whi;
+            lean_slab<TOF, false, QDIV>(E, ax, act ? ip : whi, fminf(pp0 + (float)(G * u), ppmax), act, o[u], w[u]);
+        } else {
+            o[u][0] = o[u][1] = o[u][2] = 0;
+            w[u][0] = w[u][1] = w[u][2] = 0.0f;
+        }
+    }
+}
+
 // U slabs of one chunk of a walk over slabs [c0, whi] with G lanes per LOR (slab
 // c0 + lane + G u): offsets and weights. Groups of G slabs past whi are skipped; groups inside
-// [ilo, ihi] skip the range tests.
+// [ilo, ihi] skip the range tests. When every group with an active slab is inside, one switch on
+// their number runs them as straight-line code.
 template <bool TOF, int U, int G, bool QDIV>
 __device__ __forceinline__ void lean_chunk(const LeanRec &E, const LeanAxes &ax, int c0, int whi, float ppmax,
                                            int lane, int32_t (&o)[U][3], float (&w)[U][3]) {
     const float pp0 = (float)(c0 + lane - E.ic);
+    const int ng = min(U, (whi - c0) / G + 1);  // groups with an active slab (c0 <= whi)
+    if (c0 >= E.ilo && min(c0 + G * ng - 1, whi) <= E.ihi) {
+        static_assert(U >= 1 && U <= 4, "1 to 4 groups per chunk");
+        switch (ng) {
+        case 1: lean_interior_groups<TOF, U, G, QDIV, 1>(E, ax, c0, whi, ppmax, pp0, lane, o, w); return;
+        case 2: lean_interior_groups<TOF, U, G, QDIV, (U >= 2 ? 2 : 1)>(E, ax, c0, whi, ppmax, pp0, lane, o, w); return;
+        case 3: lean_interior_groups<TOF, U, G, QDIV, (U >= 3 ? 3 : 1)>(E, ax, c0, whi, ppmax, pp0, lane, o, w); return;
+        default: lean_interior_groups<TOF, U, G, QDIV, U>(E, ax, c0, whi, ppmax, pp0, lane, o, w); return;
+        }
+    }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int g0 = c0 + G * u;  // first slab of the group (uniform over the group)
