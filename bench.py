@@ -38,7 +38,7 @@ UNIT = "LOR-voxel updates/s"
 FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes (read + write) of one k_osem_subset launch of this workload (2e6 TOF LORs of an
 # interleaved subset, clinical image), from ncu: profiles/k_osem_subset_tof_clinical_2M_lors.txt
-NCU_TRAFFIC_SUBSET = 187_251_712
+NCU_TRAFFIC_SUBSET = 187_686_144
 
 
 def parse():
