@@ -34,8 +34,10 @@
 // Range tests. Per LOR, [ilo, ihi] is the slab range whose face coordinates all lie at least
 // kInteriorMargin inside the image box, so every candidate voxel is inside. A group of 32 slabs
 // entirely within it skips the reference's range tests (siddon.cu.cc:88-189); other groups run
-// them. Gathers and reductions are predicated on a non-zero weight (a zero-weight slot still has
-// a valid address, so neither needs a range test).
+// them. A chunk whose active groups all lie within it runs them without a branch between them, so
+// that the groups' independent instruction chains interleave. Gathers and reductions are
+// predicated on a non-zero weight (a zero-weight slot still has a valid address, so neither needs
+// a range test).
 #pragma once
 #include "fused.cuh"
 
